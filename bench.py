@@ -1,0 +1,364 @@
+"""Benchmark of the girih star-stencil hot path on GB300.
+
+Workload (default): the 7-point constant-coefficient leapfrog stencil (operator
+8: u = 2v - u + roc2*(c0 v + c1 sum6 v)), nx=ny=nz=512, nt=500, seeded U(0,1)
+fields, roc2 U(0.5,1.5), c = (-0.75, 0.125); inputs FP32-representable so that
+FP32 and FP64 runs see identical data.  One benchmark "step" is one call of the
+hot path: the whole nt=500 time loop over the 512^3 grid.
+
+Forms measured on the same grid, each from device-resident inputs:
+  plain64  FP64, one sweep per kernel launch (the drop-in form)
+  fused64  FP64, time-fused passes
+  mixed    FP32 fields, compensated leapfrog, time-fused passes
+`value` is the headline form's GLUP/s (--headline, default mixed); `e2e` is the
+same form through the C ABI from pinned HOST arrays (upload + run + download).
+
+--impl reference times the CPU restatement of the reference operator (the
+oracle, OpenMP over all host cores) on a bounded sample of the same workload.
+Multi-GPU (torchrun): every rank advances its own replica of the grid
+("replicas only": the path has no exchange on one grid per GPU).
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: op, n, nt, seed, field range, roc2 range, constant coefficients
+    "star7_leapfrog_512": dict(op=8, n=512, nt=500, seed=1, f=(0.0, 1.0), roc2=(0.5, 1.5), coefs=[-0.75, 0.125]),
+    "star7_jacobi_512": dict(op=1, n=512, nt=500, seed=1, f=(0.0, 1.0), roc2=(0.0, 0.0), coefs=[-0.28472, 0.16]),
+    "star25_leapfrog_480": dict(op=0, n=480, nt=200, seed=2, f=(-1.0, 1.0), roc2=(0.05, 0.15),
+                                coefs=[-8.541667, 1.6, -0.2, 0.025396826, -0.0017857143]),
+}
+
+
+def rank_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def committed_traffic(kernel_key):
+    """DRAM bytes per launch of a kernel from the committed ncu summary, or None."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f).get(kernel_key)
+    except Exception:
+        return None
+
+
+def pass_bytes(op_info, tsz, schedule, precision):
+    """Compulsory HBM bytes per grid point of one kernel launch.
+    plain: read v (+u, roc2), write u.  fused: read cur (+prev, roc2), write two states."""
+    r, to, nc, var = op_info
+    if schedule == "plain":
+        b = 2 * tsz + (2 * tsz if to == 2 else 0)
+        if var:
+            b += nc * (2 if precision == "mixed" else tsz)
+        return b
+    return (3 * tsz + 2 * tsz) if to == 2 else (tsz + tsz)
+
+
+def run_ours(args, wl, rank, world, local):
+    import numpy as np
+    import torch
+    from girih_gb300 import gpu
+
+    torch.cuda.set_device(local)
+    n, nt, op = wl["n"], wl["nt"], wl["op"]
+    lups = float(n) ** 3 * (2 * ((nt + 1) // 2))
+    forms = {
+        "plain64": dict(precision="fp64", schedule="plain"),
+        "fused64": dict(precision="fp64", schedule="fused"),
+        "mixed": dict(precision="mixed", schedule="fused"),
+    }
+    if args.forms:
+        forms = {k: v for k, v in forms.items() if k in args.forms.split(",")}
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+
+    def barrier_sync():
+        torch.cuda.synchronize()
+        if dist:
+            tdist.barrier()
+
+    results, ctxs = {}, {}
+    sampler = ClockSampler(local)
+    with sampler:
+        for name, kw in forms.items():
+            ctx = gpu.Context(op, n, n, n, device=local, fusion_depth=args.depth if kw["schedule"] == "fused" else 0, **kw)
+            ctx.fill_seeded(wl["seed"], wl["f"], wl["roc2"], (0.0, 0.0), coefs=wl["coefs"], f32_exact=True)
+            for _ in range(args.warmup):
+                ctx.run(nt)
+            barrier_sync()
+            ms = []
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                ms.append(ctx.run(nt))
+            barrier_sync()
+            wall = time.perf_counter() - t0
+            dev_s = sum(ms) / 1e3
+            if dist:
+                t = torch.tensor([dev_s], dtype=torch.float64, device="cuda")
+                tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+                dev_s = float(t.item())
+            info = ctx.info()
+            results[name] = dict(glups=world * args.steps * lups / dev_s / 1e9, ms_per_step=1e3 * dev_s / args.steps,
+                                 wall_s=wall, launches_per_step=info["launches_last_run"],
+                                 depth=info["fusion_depth"], tile=[info["block_x"], info["block_y"]],
+                                 kernel=info["kernel_name"], tsz=8 if kw["precision"] == "fp64" else 4,
+                                 schedule=kw["schedule"], precision=kw["precision"])
+            ctxs[name] = ctx
+    clocks = sampler.summary()
+
+    # errors: fresh nt-step runs from the same init against the FP64 plain form
+    errors = {}
+    if "plain64" in forms and not args.no_error:
+        ref = gpu.Context(op, n, n, n, device=local, precision="fp64", schedule="plain")
+        ref.fill_seeded(wl["seed"], wl["f"], wl["roc2"], (0.0, 0.0), coefs=wl["coefs"], f32_exact=True)
+        ref.run(nt)
+        for name, kw in forms.items():
+            if name == "plain64":
+                continue
+            c = gpu.Context(op, n, n, n, device=local, fusion_depth=args.depth if kw["schedule"] == "fused" else 0, **kw)
+            c.fill_seeded(wl["seed"], wl["f"], wl["roc2"], (0.0, 0.0), coefs=wl["coefs"], f32_exact=True)
+            c.run(nt)
+            mr, l2 = gpu.rel_errors(c.compare(ref))
+            errors[name] = {"max_rel": mr, "l2_rel": l2, "nt": nt, "against": "plain64 (FP64, parity-checked vs the oracle)"}
+            c.close()
+        ref.close()
+
+    head = args.headline if args.headline in results else list(results)[0]
+    h = results[head]
+    # roofline of the headline form's kernel (one launch = one pass over the grid)
+    peak, peak_kind = measured_peak_hbm()
+    op_info = gpu.OP_INFO[op]
+    per_pt = pass_bytes(op_info, h["tsz"], h["schedule"], h["precision"])
+    launch_ms = h["ms_per_step"] / max(1, h["launches_per_step"])
+    achieved = per_pt * float(n) ** 3 / (launch_ms / 1e3) / 1e9
+    kernel_key = f"{h['kernel']}:{WORKLOAD_NAME}:{head}"
+    traffic = committed_traffic(kernel_key)
+
+    # end to end through the C ABI from pinned host arrays
+    e2e = None
+    if not args.no_e2e:
+        ctx = ctxs[head]
+        shape = ctx.shape
+        host = [torch.empty(shape, dtype=torch.float64, pin_memory=True) for _ in range(3)]
+        # fill the host arrays with the seeded inputs: download the initial state
+        init = gpu.Context(op, n, n, n, device=local, precision="fp64", schedule="plain")
+        init.fill_seeded(wl["seed"], wl["f"], wl["roc2"], (0.0, 0.0), coefs=wl["coefs"], f32_exact=True)
+        init.download(host[0].data_ptr(), host[1].data_ptr())
+        init.download_roc2(host[2].data_ptr()) if op_info[1] == 2 else None
+        init.close()
+        coefs = np.array(wl["coefs"] + [0.0] * (11 - len(wl["coefs"])))
+        ctx.close()
+        ectx = gpu.Context(op, n, n, n, device=local, fusion_depth=args.depth if forms[head]["schedule"] == "fused" else 0,
+                           **forms[head])
+        u3 = host[2].data_ptr() if op_info[1] == 2 else None
+        for _ in range(max(1, args.warmup)):
+            ectx.upload(host[0].data_ptr(), host[1].data_ptr(), u3, coefs)
+            ectx.run(nt)
+            ectx.download(host[0].data_ptr(), None)
+        barrier_sync()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            ectx.upload(host[0].data_ptr(), host[1].data_ptr(), u3, coefs)
+            ectx.run(nt)
+            ectx.download(host[0].data_ptr(), None)
+        barrier_sync()
+        wall = time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([wall], dtype=torch.float64, device="cuda")
+            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+            wall = float(t.item())
+        nbytes = host[0].numel() * 8
+        e2e = {"value": world * args.steps * lups / wall / 1e9, "unit": "GLUP/s",
+               "h2d_bytes_per_step": nbytes * (3 if u3 else 2), "d2h_bytes_per_step": nbytes,
+               "host_arrays": "pinned FP64 (reference real_t=double layout)"}
+        ectx.close()
+    for c in ctxs.values():
+        c.close()
+
+    line = {
+        "metric": "GLUP/s at 512^3: time-fused & mixed vs plain FP64 on GB300; % HBM roofline; err",
+        "value": h["glups"], "unit": "GLUP/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": h["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if h["precision"] != "fp64" else "f64", "data": "synthetic (seeded SplitMix64, FP32-representable)",
+        "config": {"workload": WORKLOAD_NAME, "operator": op, "grid": [n, n, n], "nt": nt, "headline_form": head,
+                   "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (no flush needed)"},
+        "forms": {k: {kk: v[kk] for kk in ("glups", "ms_per_step", "launches_per_step", "depth", "tile")}
+                  for k, v in results.items()},
+        "errors": errors,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": peak_kind, "kernel": h["kernel"],
+                     "algorithmic_bytes_per_point_per_launch": per_pt,
+                     "effective_bandwidth_gbs": h["glups"] * (per_pt if h["schedule"] == "plain" else
+                                                              pass_bytes(op_info, h["tsz"], "plain", h["precision"]))},
+        "e2e": e2e,
+        "gpu_launches": args.steps * h["launches_per_step"],
+        "clocks": clocks,
+    }
+    if "plain64" in results:
+        line["speedup_vs_plain64"] = {k: v["glups"] / results["plain64"]["glups"] for k, v in results.items()}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
+    return line
+
+
+def cpu_baseline(wl, seconds, steps=None):
+    """The oracle restatement (OpenMP over all host threads) on a bounded sample of
+    the workload: the full grid, a few sweeps.  Returns the cpu_baseline object."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    n, op = wl["n"], wl["op"]
+    threads = os.cpu_count() or 1
+    g = oracle.Grid(op, n, n, n)
+    g.fill_seeded(wl["seed"], wl["f"], wl["roc2"], coefs=wl["coefs"], nthreads=threads)
+    t0 = time.perf_counter()
+    g.run(2, nthreads=threads)
+    per_pair = time.perf_counter() - t0
+    pairs = steps if steps else max(1, int(seconds / max(per_pair, 1e-3)))
+    t0 = time.perf_counter()
+    g.run(2 * pairs, nthreads=threads)
+    dt = time.perf_counter() - t0
+    glups = float(n) ** 3 * 2 * pairs / dt / 1e9
+    return {"value": glups, "unit": "GLUP/s", "cores": threads, "kind": "port",
+            "sample": f"{n}^3 grid, {2 * pairs} sweeps of operator {op} ({dt:.1f} s)"}
+
+
+def run_reference(args, wl, rank, world):
+    if rank != 0:
+        return None
+    vals = []
+    for _ in range(args.warmup):
+        pass  # the CPU restatement has no warm-up state beyond its first sweeps
+    threads = os.cpu_count() or 1
+    per_step_s = max(1.0, args.cpu_seconds / max(1, args.steps))
+    cb = None
+    for _ in range(args.steps):
+        cb = cpu_baseline(wl, per_step_s)
+        vals.append(cb["value"])
+    v = statistics.median(vals)
+    cb["value"] = v
+    return {"impl": "reference", "metric": "GLUP/s at 512^3: time-fused & mixed vs plain FP64 on GB300; % HBM roofline; err",
+            "value": v, "unit": "GLUP/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD_NAME, "operator": wl["op"], "grid": [wl["n"]] * 3, "nt": wl["nt"],
+                       "threads": threads},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": "GLUP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+WORKLOAD_NAME = "star7_leapfrog_512"
+
+
+def main():
+    global WORKLOAD_NAME
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="star7_leapfrog_512", choices=sorted(WORKLOADS))
+    ap.add_argument("--forms", default="")
+    ap.add_argument("--headline", default="mixed")
+    ap.add_argument("--depth", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-error", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    WORKLOAD_NAME = args.workload
+    wl = WORKLOADS[args.workload]
+    rank, world, local = rank_env()
+    if world > 1 and args.impl == "ours":
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl")
+    if args.impl == "reference":
+        line = run_reference(args, wl, rank, world)
+    else:
+        line = run_ours(args, wl, rank, world, local)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1 and args.impl == "ours":
+        import torch.distributed as tdist
+        tdist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

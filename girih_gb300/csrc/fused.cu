@@ -1,0 +1,71 @@
+// Fused-schedule dispatch: which operators have a time-fused kernel, the tile
+// and depth for a grid, and the launch routed to the per-operator instantiations.
+#include "fused.cuh"
+
+namespace girih {
+
+bool fused_supported(const Geom &g, int precision) {
+  (void)precision;
+  return g.op == 0 || g.op == 1 || g.op == 8;
+}
+
+int fused_max_depth(const Geom &g, int precision) {
+  if (g.r == 4) return 2;
+  return precision == GIRIH_FP64 ? 4 : 6;
+}
+
+// Column region of one CTA: variant 0 = 64 x 32 (64x16 threads, 2 rows each),
+// variant 1 = 32 x 64 (32x16 threads, 4 rows each).
+static void variant_shape(int v, int *ntx, int *ry) {
+  *ntx = v == 0 ? 64 : 32;
+  *ry = v == 0 ? 32 : 64;
+}
+
+FusedConfig make_fused_config(const Geom &g, int precision, int depth, int variant) {
+  FusedConfig c{};
+  if (!fused_supported(g, precision) || depth < 1 || depth > fused_max_depth(g, precision) ||
+      variant < 0 || variant >= FV_COUNT)
+    return c;
+  int ntx, ry;
+  variant_shape(variant, &ntx, &ry);
+  c.depth = depth;
+  c.variant = variant;
+  c.bx = ntx - 2 * depth * g.r;
+  c.by = ry - 2 * depth * g.r;
+  if (c.bx <= 0 || c.by <= 0) c.depth = 0;
+  return c;
+}
+
+FusedConfig choose_fused_config(const Geom &g, int precision, int depth, int bx, int by) {
+  int d = depth;
+  if (d <= 0) d = g.r == 4 ? 2 : (precision == GIRIH_FP64 ? 2 : 4);
+  d = d > fused_max_depth(g, precision) ? fused_max_depth(g, precision) : d;
+  for (int v = 0; v < FV_COUNT; v++) {
+    FusedConfig c = make_fused_config(g, precision, d, v);
+    if (!c.depth) continue;
+    if ((bx && bx != c.bx) || (by && by != c.by)) continue;
+    return c;
+  }
+  return FusedConfig{};
+}
+
+cudaError_t launch_fused(const Geom &g, int tsz, int precision, const FusedConfig &cfg,
+                         const FusedLaunch &L, cudaStream_t s) {
+  const bool comp = precision == GIRIH_MIXED && g.to == 2;
+  switch (g.op) {
+    case 1:
+      return tsz == 8 ? launch_fused_op<1, double, false>(g, cfg, L, s)
+                      : launch_fused_op<1, float, false>(g, cfg, L, s);
+    case 8:
+      if (tsz == 8) return launch_fused_op<8, double, false>(g, cfg, L, s);
+      return comp ? launch_fused_op<8, float, true>(g, cfg, L, s) : launch_fused_op<8, float, false>(g, cfg, L, s);
+    case 0:
+      if (tsz == 8) return launch_fused_op<0, double, false>(g, cfg, L, s);
+      return comp ? launch_fused_op<0, float, true>(g, cfg, L, s) : launch_fused_op<0, float, false>(g, cfg, L, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+const char *fused_kernel_name() { return "fused_pass"; }
+
+}  // namespace girih

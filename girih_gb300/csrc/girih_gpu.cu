@@ -1,0 +1,647 @@
+// C-ABI entry points of libgirih_gpu (declared in include/girih_gpu.h).
+//
+// A context holds one grid on one device: field buffers in the device layout
+// (see Geom), roc2, coefficients, a staging buffer for host-layout conversion
+// and a stream.  run() replays a captured CUDA graph of the whole time loop
+// between two CUDA events on that stream, which replaces the reference's
+// MPI_Wtime bracket around the stepper (src/performance.c:74-78).
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "internal.cuh"
+#include "fused.cuh"
+
+namespace girih {
+
+static thread_local std::string g_last_error;
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+int op_info(int op, int *r, int *to, int *nc, int *var) {
+  int R, TO, NC, VAR;
+  switch (op) {  // src/kernels/stencils.c:260-271
+    case 0: R = 4; TO = 2; NC = 5; VAR = 0; break;
+    case 1: R = 1; TO = 1; NC = 2; VAR = 0; break;
+    case 2: R = 1; TO = 1; NC = 2; VAR = 1; break;
+    case 3: R = 1; TO = 1; NC = 4; VAR = 1; break;
+    case 4: R = 4; TO = 1; NC = 13; VAR = 1; break;
+    case 5: R = 1; TO = 1; NC = 7; VAR = 1; break;
+    case 8: R = 1; TO = 2; NC = 2; VAR = 0; break;
+    default: return -1;
+  }
+  if (r) *r = R;
+  if (to) *to = TO;
+  if (nc) *nc = NC;
+  if (var) *var = VAR;
+  return 0;
+}
+
+Geom make_geom(int op, int nx, int ny, int nz, int hpx, int tsz) {
+  Geom g{};
+  op_info(op, &g.r, &g.to, &g.nc, &g.var);
+  g.op = op;
+  g.nx = nx; g.ny = ny; g.nz = nz;
+  g.nnx = nx + 2 * g.r; g.nny = ny + 2 * g.r; g.nnz = nz + 2 * g.r;
+  g.hpx = hpx;
+  const int A = 128 / tsz;  // elements per 128 bytes
+  g.ox = (A - (g.r % A)) % A;
+  g.px = ((g.ox + g.nnx + A - 1) / A) * A;
+  g.plane = (int64_t)g.px * g.nny;
+  g.elems = g.plane * g.nnz;
+  return g;
+}
+
+}  // namespace girih
+
+using namespace girih;
+
+struct girih_gpu_ctx {
+  girih_gpu_desc d{};
+  Geom g{};
+  int tsz = 8, hsz = 8;
+  bool bf16coef = false;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  void *f[4] = {nullptr, nullptr, nullptr, nullptr};  // field buffers
+  int iu1 = 0, iu2 = 1;                               // buffers holding U1 and U2
+  void *roc2 = nullptr;
+  void *coef = nullptr;
+  float *scale = nullptr;
+  double cc[5] = {0, 0, 0, 0, 0};
+  void *staging = nullptr;
+  size_t staging_bytes = 0;
+  double *acc = nullptr;  // 4 doubles for norms, then flag words
+  bool uploaded = false;
+  bool halos_equal = false;
+  int sched = GIRIH_SCHED_PLAIN;
+  FusedConfig fcfg{};
+  cudaGraphExec_t gexec = nullptr;
+  int g_steps = -1, g_iu1 = -1, g_iu2 = -1;
+  int g_launches = 0, g_new_iu1 = 0, g_new_iu2 = 1;
+  int last_launches = 0, last_steps = 0;
+  double dev_bytes = 0;
+};
+
+namespace {
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+#define CK(...)                                                                    \
+  do {                                                                             \
+    cudaError_t e_ = (__VA_ARGS__);                                                \
+    if (e_ != cudaSuccess) {                                                       \
+      set_error(std::string(#__VA_ARGS__) + ": " + cudaGetErrorString(e_));        \
+      return e_ == cudaErrorMemoryAllocation ? GIRIH_GPU_ENOMEM : GIRIH_GPU_ECUDA; \
+    }                                                                              \
+  } while (0)
+
+int fail(int code, const std::string &msg) {
+  set_error(msg);
+  return code;
+}
+
+int dev_alloc(girih_gpu_ctx *c, void **p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    return fail(GIRIH_GPU_ENOMEM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed: " +
+                                      cudaGetErrorString(e));
+  }
+  c->dev_bytes += (double)bytes;
+  CK(cudaMemsetAsync(*p, 0, bytes, c->st));
+  return 0;
+}
+
+int ensure_staging(girih_gpu_ctx *c, size_t bytes) {
+  if (c->staging_bytes >= bytes) return 0;
+  if (c->staging) {
+    cudaFree(c->staging);
+    c->dev_bytes -= (double)c->staging_bytes;
+    c->staging = nullptr;
+    c->staging_bytes = 0;
+  }
+  int e = dev_alloc(c, &c->staging, bytes);
+  if (!e) c->staging_bytes = bytes;
+  return e;
+}
+
+size_t host_array_elems(const girih_gpu_ctx *c) {
+  return (size_t)c->d.ldomain_shape[0] * c->d.ldomain_shape[1] * c->d.ldomain_shape[2];
+}
+
+// Host (reference layout, element size hsz) -> device layout buffer (tsz).
+int upload_field(girih_gpu_ctx *c, const void *h, void *dst) {
+  const Geom &g = c->g;
+  if (c->hsz == c->tsz) {
+    CK(cudaMemcpy2DAsync(static_cast<char *>(dst) + (size_t)g.ox * c->tsz, (size_t)g.px * c->tsz, h,
+                         (size_t)g.hpx * c->hsz, (size_t)g.nnx * c->tsz, (size_t)g.nny * g.nnz,
+                         cudaMemcpyHostToDevice, c->st));
+    return 0;
+  }
+  size_t n = host_array_elems(c);
+  int e = ensure_staging(c, n * 8);
+  if (e) return e;
+  CK(cudaMemcpyAsync(c->staging, h, n * c->hsz, cudaMemcpyHostToDevice, c->st));
+  if (c->hsz == 8)
+    CK(launch_to_device_layout<double, float>(g, (const double *)c->staging, (float *)dst, c->st));
+  else
+    CK(launch_to_device_layout<float, double>(g, (const float *)c->staging, (double *)dst, c->st));
+  return 0;
+}
+
+int download_field(girih_gpu_ctx *c, const void *src, void *h) {
+  const Geom &g = c->g;
+  if (c->hsz == c->tsz) {
+    CK(cudaMemcpy2DAsync(h, (size_t)g.hpx * c->hsz, static_cast<const char *>(src) + (size_t)g.ox * c->tsz,
+                         (size_t)g.px * c->tsz, (size_t)g.nnx * c->tsz, (size_t)g.nny * g.nnz,
+                         cudaMemcpyDeviceToHost, c->st));
+    return 0;
+  }
+  size_t n = host_array_elems(c);
+  int e = ensure_staging(c, n * 8);
+  if (e) return e;
+  if (c->hsz == 8)
+    CK(launch_to_host_layout<float, double>(g, (const float *)src, (double *)c->staging, c->st));
+  else
+    CK(launch_to_host_layout<double, float>(g, (const double *)src, (float *)c->staging, c->st));
+  CK(cudaMemcpy2DAsync(h, (size_t)g.hpx * c->hsz, c->staging, (size_t)g.hpx * c->hsz,
+                       (size_t)g.nnx * c->hsz, (size_t)g.nny * g.nnz, cudaMemcpyDeviceToHost, c->st));
+  return 0;
+}
+
+// Quantise coefficient array m (host layout, already in staging as Tin) to BF16.
+template <class Tin>
+int quantize_from_staging(girih_gpu_ctx *c, int m) {
+  unsigned long long *mx = reinterpret_cast<unsigned long long *>(c->acc + 4);
+  CK(cudaMemsetAsync(mx, 0, 8, c->st));
+  CK(launch_maxabs<Tin>(c->g, (const Tin *)c->staging, mx, c->st));
+  unsigned long long bits = 0;
+  CK(cudaMemcpyAsync(&bits, mx, 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  double mxv;
+  std::memcpy(&mxv, &bits, 8);
+  float s = (mxv > 0 && mxv == mxv) ? (float)mxv : 1.0f;
+  CK(cudaMemcpyAsync(c->scale + m, &s, 4, cudaMemcpyHostToDevice, c->st));
+  __nv_bfloat16 *dst = static_cast<__nv_bfloat16 *>(c->coef) + (size_t)m * c->g.elems;
+  CK(launch_quantize_bf16<Tin>(c->g, (const Tin *)c->staging, dst, c->scale + m, c->st));
+  CK(cudaStreamSynchronize(c->st));  // the host scale value must outlive the copy
+  return 0;
+}
+
+int check_halos(girih_gpu_ctx *c) {
+  unsigned int *flag = reinterpret_cast<unsigned int *>(c->acc + 5);
+  CK(cudaMemsetAsync(flag, 0, 4, c->st));
+  CK(launch_halo_equal(c->g, c->f[0], c->f[1], c->tsz, flag, c->st));
+  unsigned int h = 1;
+  CK(cudaMemcpyAsync(&h, flag, 4, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->halos_equal = (h == 0);
+  return 0;
+}
+
+void drop_graph(girih_gpu_ctx *c) {
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  c->gexec = nullptr;
+  c->g_steps = -1;
+}
+
+// Extra field buffers for the fused schedule: inputs and outputs of a fused
+// pass must differ because neighbouring tiles read overlapping halos.
+int ensure_fused_buffers(girih_gpu_ctx *c) {
+  for (int b = 2; b < 4; b++) {
+    if (!c->f[b]) {
+      int e = dev_alloc(c, &c->f[b], (size_t)c->g.elems * c->tsz);
+      if (e) return e;
+    }
+  }
+  return 0;
+}
+
+template <class T> StepArgs<T> step_args(girih_gpu_ctx *c, void *u, const void *v) {
+  StepArgs<T> a{};
+  a.g = c->g;
+  a.u = static_cast<T *>(u);
+  a.v = static_cast<const T *>(v);
+  a.roc2 = static_cast<const T *>(c->roc2);
+  a.coef = c->coef;
+  a.scale = c->scale;
+  for (int m = 0; m < 5; m++) a.cc[m] = (T)c->cc[m];
+  return a;
+}
+
+// Issue the launches of `steps` time steps on the context stream (captured
+// into a graph by the caller).  Plain: U1 <- op(U2), U2 <- op(U1) in place of
+// the reference's two sweeps per iteration.  Fused: passes of depth T rotate
+// through the four field buffers.
+int issue_steps(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *iu2) {
+  *launches = 0;
+  const bool exact = c->d.exact != 0;
+  if (c->sched == GIRIH_SCHED_PLAIN) {
+    for (int s = 0; s < steps; s += 2) {
+      for (int h = 0; h < 2; h++) {
+        void *u = c->f[h == 0 ? *iu1 : *iu2];
+        const void *v = c->f[h == 0 ? *iu2 : *iu1];
+        cudaError_t e = c->tsz == 8 ? launch_plain<double>(step_args<double>(c, u, v), exact, false, c->st)
+                                    : launch_plain<float>(step_args<float>(c, u, v), exact, c->bf16coef, c->st);
+        if (e != cudaSuccess) return fail(GIRIH_GPU_ECUDA, std::string("plain launch: ") + cudaGetErrorString(e));
+        (*launches)++;
+      }
+    }
+    return 0;
+  }
+  // fused: state S-1 in buffer iu1, state S in iu2; each pass writes the two
+  // newest states into the two spare buffers
+  int left = steps;
+  while (left > 0) {
+    int T = std::min(left, c->fcfg.depth);
+    int spare[2], n = 0;
+    for (int b = 0; b < 4 && n < 2; b++)
+      if (b != *iu1 && b != *iu2) spare[n++] = b;
+    FusedLaunch L{};
+    L.prev = c->f[*iu1];
+    L.cur = c->f[*iu2];
+    L.out_prev = c->f[spare[0]];
+    L.out_cur = c->f[spare[1]];
+    L.roc2 = c->roc2;
+    L.steps = T;
+    // time order 1 never reads state t-1, so only the last pass writes it (U1)
+    L.write_prev = (c->g.to == 2 || left == T) ? 1 : 0;
+    for (int m = 0; m < 5; m++) L.cc[m] = c->cc[m];
+    cudaError_t e = launch_fused(c->g, c->tsz, c->d.precision, c->fcfg, L, c->st);
+    if (e != cudaSuccess) return fail(GIRIH_GPU_ECUDA, std::string("fused launch: ") + cudaGetErrorString(e));
+    (*launches)++;
+    *iu1 = spare[0];
+    *iu2 = spare[1];
+    left -= T;
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int girih_gpu_abi_version(void) { return GIRIH_GPU_ABI_VERSION; }
+
+const char *girih_gpu_strerror(int err) {
+  switch (err) {
+    case GIRIH_GPU_OK: return "success";
+    case GIRIH_GPU_EINVAL: return "invalid argument";
+    case GIRIH_GPU_EUNSUPPORTED: return "unsupported operator/precision/schedule combination";
+    case GIRIH_GPU_ECUDA: return "CUDA runtime error";
+    case GIRIH_GPU_ENOMEM: return "device out of memory";
+    case GIRIH_GPU_ESTATE: return "call out of order";
+    case GIRIH_GPU_ETIMEOUT: return "device-side wait timed out";
+    case GIRIH_GPU_ENODEV: return "no usable CUDA device";
+  }
+  return "unknown error";
+}
+
+const char *girih_gpu_last_error(void) { return g_last_error.c_str(); }
+
+int girih_gpu_create(girih_gpu_ctx **out, const girih_gpu_desc *d) {
+  if (!out || !d) return fail(GIRIH_GPU_EINVAL, "null argument");
+  *out = nullptr;
+  int r, to, nc, var;
+  if (op_info(d->target_kernel, &r, &to, &nc, &var))
+    return fail(GIRIH_GPU_EUNSUPPORTED, "operator id " + std::to_string(d->target_kernel) +
+                                            " is not a star operator provided on the GPU");
+  const int nx = d->stencil_shape[0], ny = d->stencil_shape[1], nz = d->stencil_shape[2];
+  if (nx < 1 || ny < 1 || nz < 1) return fail(GIRIH_GPU_EINVAL, "interior extents must be >= 1");
+  if (d->ldomain_shape[0] < nx + 2 * r || d->ldomain_shape[1] != ny + 2 * r || d->ldomain_shape[2] != nz + 2 * r)
+    return fail(GIRIH_GPU_EINVAL, "ldomain_shape must be (>= nx+2r, ny+2r, nz+2r)");
+  if (d->host_real_size != 4 && d->host_real_size != 8) return fail(GIRIH_GPU_EINVAL, "host_real_size must be 4 or 8");
+  if (d->precision < GIRIH_FP64 || d->precision > GIRIH_MIXED) return fail(GIRIH_GPU_EINVAL, "bad precision");
+  if (d->schedule < GIRIH_SCHED_PLAIN || d->schedule > GIRIH_SCHED_AUTO) return fail(GIRIH_GPU_EINVAL, "bad schedule");
+  if ((int64_t)d->ldomain_shape[0] * d->ldomain_shape[1] > (int64_t)1 << 31)
+    return fail(GIRIH_GPU_EINVAL, "x-y plane too large");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return fail(GIRIH_GPU_ENODEV, "no CUDA device");
+  }
+  if (d->device < 0 || d->device >= ndev) return fail(GIRIH_GPU_EINVAL, "device ordinal out of range");
+  DeviceGuard dg(d->device);
+
+  girih_gpu_ctx *c = new (std::nothrow) girih_gpu_ctx;
+  if (!c) return fail(GIRIH_GPU_ENOMEM, "host allocation failed");
+  c->d = *d;
+  c->tsz = d->precision == GIRIH_FP64 ? 8 : 4;
+  c->hsz = d->host_real_size;
+  c->bf16coef = d->precision == GIRIH_MIXED && var;
+  c->g = make_geom(d->target_kernel, nx, ny, nz, d->ldomain_shape[0], c->tsz);
+
+  // schedule selection
+  int sched = d->schedule;
+  if (sched != GIRIH_SCHED_PLAIN) {
+    bool ok = fused_supported(c->g, d->precision);
+    if (sched == GIRIH_SCHED_FUSED && !ok) {
+      delete c;
+      return fail(GIRIH_GPU_EUNSUPPORTED, "no fused kernel for this operator/precision");
+    }
+    if (sched == GIRIH_SCHED_FUSED && d->exact) {
+      delete c;
+      return fail(GIRIH_GPU_EUNSUPPORTED, "exact rounding is provided by the plain schedule only");
+    }
+    sched = ok && !d->exact ? GIRIH_SCHED_FUSED : GIRIH_SCHED_PLAIN;
+  }
+  c->sched = sched;
+  if (sched == GIRIH_SCHED_FUSED) {
+    c->fcfg = choose_fused_config(c->g, d->precision, d->fusion_depth, d->block_x, d->block_y);
+    if (!c->fcfg.depth) {
+      delete c;
+      return fail(GIRIH_GPU_EUNSUPPORTED, "requested fused tile/depth is not provided");
+    }
+  }
+
+  int e = 0;
+  auto bail = [&](int code) {
+    girih_gpu_destroy(c);
+    return code;
+  };
+  if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->e0) != cudaSuccess || cudaEventCreate(&c->e1) != cudaSuccess) {
+    cudaGetLastError();
+    return bail(fail(GIRIH_GPU_ECUDA, "stream/event creation failed"));
+  }
+  const size_t fb = (size_t)c->g.elems * c->tsz;
+  if ((e = dev_alloc(c, &c->f[0], fb)) || (e = dev_alloc(c, &c->f[1], fb))) return bail(e);
+  if (to == 2 && (e = dev_alloc(c, &c->roc2, fb))) return bail(e);
+  if (var) {
+    size_t cb = (size_t)c->g.elems * nc * (c->bf16coef ? 2 : c->tsz);
+    if ((e = dev_alloc(c, &c->coef, cb))) return bail(e);
+    if (c->bf16coef && (e = dev_alloc(c, (void **)&c->scale, 64 * sizeof(float)))) return bail(e);
+  }
+  if ((e = dev_alloc(c, (void **)&c->acc, 64))) return bail(e);
+  if (sched == GIRIH_SCHED_FUSED && (e = ensure_fused_buffers(c))) return bail(e);
+  if (cudaStreamSynchronize(c->st) != cudaSuccess) return bail(fail(GIRIH_GPU_ECUDA, "initial clear failed"));
+  *out = c;
+  return 0;
+}
+
+void girih_gpu_destroy(girih_gpu_ctx *c) {
+  if (!c) return;
+  DeviceGuard dg(c->d.device);
+  if (c->st) cudaStreamSynchronize(c->st);
+  drop_graph(c);
+  for (void *p : c->f)
+    if (p) cudaFree(p);
+  if (c->roc2) cudaFree(c->roc2);
+  if (c->coef) cudaFree(c->coef);
+  if (c->scale) cudaFree(c->scale);
+  if (c->staging) cudaFree(c->staging);
+  if (c->acc) cudaFree(c->acc);
+  if (c->e0) cudaEventDestroy(c->e0);
+  if (c->e1) cudaEventDestroy(c->e1);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+}
+
+int girih_gpu_upload(girih_gpu_ctx *c, const void *U1, const void *U2, const void *U3, const void *coef) {
+  if (!c || !U1 || !U2) return fail(GIRIH_GPU_EINVAL, "null context or field array");
+  const Geom &g = c->g;
+  if (g.to == 2 && !U3) return fail(GIRIH_GPU_EINVAL, "time-order-2 operator needs U3 (roc2)");
+  if (!coef) return fail(GIRIH_GPU_EINVAL, "null coefficient array");
+  DeviceGuard dg(c->d.device);
+  drop_graph(c);
+  c->uploaded = false;
+  int e;
+  if ((e = upload_field(c, U1, c->f[0])) || (e = upload_field(c, U2, c->f[1]))) return e;
+  if (g.to == 2 && (e = upload_field(c, U3, c->roc2))) return e;
+  if (!g.var) {
+    for (int m = 0; m < 5; m++)
+      c->cc[m] = m <= g.r ? (c->hsz == 8 ? static_cast<const double *>(coef)[m]
+                                         : (double)static_cast<const float *>(coef)[m])
+                          : 0.0;
+  } else {
+    const size_t n = host_array_elems(c);
+    for (int m = 0; m < g.nc; m++) {
+      const char *src = static_cast<const char *>(coef) + (size_t)m * n * c->hsz;
+      if (!c->bf16coef) {
+        if ((e = upload_field(c, src, static_cast<char *>(c->coef) + (size_t)m * g.elems * c->tsz))) return e;
+      } else {
+        if ((e = ensure_staging(c, n * 8))) return e;
+        CK(cudaMemcpyAsync(c->staging, src, n * c->hsz, cudaMemcpyHostToDevice, c->st));
+        if ((e = c->hsz == 8 ? quantize_from_staging<double>(c, m) : quantize_from_staging<float>(c, m))) return e;
+      }
+    }
+  }
+  c->iu1 = 0;
+  c->iu2 = 1;
+  if ((e = check_halos(c))) return e;
+  if (c->sched == GIRIH_SCHED_FUSED && !c->halos_equal)
+    return fail(GIRIH_GPU_EUNSUPPORTED,
+                "fused schedule needs identical U1/U2 halos (the reference initialises them equal)");
+  if (c->sched == GIRIH_SCHED_FUSED) {
+    // every buffer carries the fixed halo
+    for (int b = 2; b < 4; b++)
+      CK(cudaMemcpyAsync(c->f[b], c->f[1], (size_t)g.elems * c->tsz, cudaMemcpyDeviceToDevice, c->st));
+  }
+  CK(cudaStreamSynchronize(c->st));
+  c->uploaded = true;
+  return 0;
+}
+
+int girih_gpu_fill_seeded(girih_gpu_ctx *c, uint64_t seed, const double ranges[6], const double *const_coefs,
+                          int flags) {
+  if (!c || !ranges) return fail(GIRIH_GPU_EINVAL, "null argument");
+  const Geom &g = c->g;
+  if (!g.var && !const_coefs) return fail(GIRIH_GPU_EINVAL, "constant operator needs const_coefs");
+  DeviceGuard dg(c->d.device);
+  drop_graph(c);
+  c->uploaded = false;
+  const int rf = (flags & GIRIH_SEED_F32_EXACT) ? 1 : 0;
+  if (c->tsz == 8) {
+    CK(launch_seeded<double>(g, seed, 0, ranges[0], ranges[1], rf, (double *)c->f[0], nullptr, c->st));
+    if (g.to == 2) CK(launch_seeded<double>(g, seed, 1, ranges[2], ranges[3], rf, (double *)c->roc2, nullptr, c->st));
+  } else {
+    CK(launch_seeded<float>(g, seed, 0, ranges[0], ranges[1], rf, (float *)c->f[0], nullptr, c->st));
+    if (g.to == 2) CK(launch_seeded<float>(g, seed, 1, ranges[2], ranges[3], rf, (float *)c->roc2, nullptr, c->st));
+  }
+  CK(cudaMemcpyAsync(c->f[1], c->f[0], (size_t)g.elems * c->tsz, cudaMemcpyDeviceToDevice, c->st));
+  if (g.var) {
+    for (int m = 0; m < g.nc; m++) {
+      if (!c->bf16coef) {
+        void *dst = static_cast<char *>(c->coef) + (size_t)m * g.elems * c->tsz;
+        if (c->tsz == 8)
+          CK(launch_seeded<double>(g, seed, 2 + m, ranges[4], ranges[5], rf, (double *)dst, nullptr, c->st));
+        else
+          CK(launch_seeded<float>(g, seed, 2 + m, ranges[4], ranges[5], rf, (float *)dst, nullptr, c->st));
+      } else {
+        int e = ensure_staging(c, host_array_elems(c) * 8);
+        if (e) return e;
+        CK(launch_seeded<float>(g, seed, 2 + m, ranges[4], ranges[5], rf, nullptr, (double *)c->staging, c->st));
+        if ((e = quantize_from_staging<double>(c, m))) return e;
+      }
+    }
+  } else {
+    for (int m = 0; m < 5; m++) c->cc[m] = m <= g.r ? const_coefs[m] : 0.0;
+  }
+  c->iu1 = 0;
+  c->iu2 = 1;
+  c->halos_equal = true;
+  if (c->sched == GIRIH_SCHED_FUSED)
+    for (int b = 2; b < 4; b++)
+      CK(cudaMemcpyAsync(c->f[b], c->f[1], (size_t)g.elems * c->tsz, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->uploaded = true;
+  return 0;
+}
+
+int girih_gpu_run(girih_gpu_ctx *c, int nt, float *ms_out) {
+  if (!c) return fail(GIRIH_GPU_EINVAL, "null context");
+  if (!c->uploaded) return fail(GIRIH_GPU_ESTATE, "run before upload");
+  if (nt < 0) return fail(GIRIH_GPU_EINVAL, "nt must be >= 0");
+  DeviceGuard dg(c->d.device);
+  const int steps = 2 * ((nt + 1) / 2);  // for(it=0; it<nt; it+=2): two sweeps each
+  if (!c->gexec || c->g_steps != steps || c->g_iu1 != c->iu1 || c->g_iu2 != c->iu2) {
+    drop_graph(c);
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeRelaxed));
+    int launches = 0, a = c->iu1, b = c->iu2;
+    int e = issue_steps(c, steps, &launches, &a, &b);
+    cudaError_t ce = cudaStreamEndCapture(c->st, &graph);
+    if (e) {
+      if (graph) cudaGraphDestroy(graph);
+      return e;
+    }
+    if (ce != cudaSuccess) return fail(GIRIH_GPU_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+    ce = cudaGraphInstantiate(&c->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) {
+      c->gexec = nullptr;
+      return fail(GIRIH_GPU_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
+    }
+    c->g_steps = steps;
+    c->g_iu1 = c->iu1;
+    c->g_iu2 = c->iu2;
+    c->g_launches = launches;
+    c->g_new_iu1 = a;
+    c->g_new_iu2 = b;
+  }
+  CK(cudaEventRecord(c->e0, c->st));
+  if (steps > 0) CK(cudaGraphLaunch(c->gexec, c->st));
+  CK(cudaEventRecord(c->e1, c->st));
+  CK(cudaEventSynchronize(c->e1));
+  CK(cudaGetLastError());
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, c->e0, c->e1));
+  if (ms_out) *ms_out = ms;
+  c->iu1 = c->g_new_iu1;
+  c->iu2 = c->g_new_iu2;
+  c->last_launches = steps > 0 ? c->g_launches : 0;
+  c->last_steps = steps;
+  return 0;
+}
+
+int girih_gpu_download(girih_gpu_ctx *c, void *U1, void *U2) {
+  if (!c) return fail(GIRIH_GPU_EINVAL, "null context");
+  if (!c->uploaded) return fail(GIRIH_GPU_ESTATE, "download before upload");
+  DeviceGuard dg(c->d.device);
+  int e;
+  if (U1 && (e = download_field(c, c->f[c->iu1], U1))) return e;
+  if (U1 && U2 && c->hsz != c->tsz) CK(cudaStreamSynchronize(c->st));  // staging reuse
+  if (U2 && (e = download_field(c, c->f[c->iu2], U2))) return e;
+  CK(cudaStreamSynchronize(c->st));
+  return 0;
+}
+
+int girih_gpu_download_roc2(girih_gpu_ctx *c, void *U3) {
+  if (!c || !U3) return fail(GIRIH_GPU_EINVAL, "null argument");
+  if (c->g.to != 2) return fail(GIRIH_GPU_EINVAL, "operator has no roc2 array");
+  if (!c->uploaded) return fail(GIRIH_GPU_ESTATE, "download before upload");
+  DeviceGuard dg(c->d.device);
+  int e = download_field(c, c->roc2, U3);
+  if (e) return e;
+  CK(cudaStreamSynchronize(c->st));
+  return 0;
+}
+
+static int read_norms(girih_gpu_ctx *c, double out[4]) {
+  double h[4];
+  CK(cudaMemcpyAsync(h, c->acc, 32, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  for (int i = 0; i < 4; i++) out[i] = h[i];
+  return 0;
+}
+
+int girih_gpu_error_norms(girih_gpu_ctx *c, const void *ref_U1, double out[4]) {
+  if (!c || !ref_U1 || !out) return fail(GIRIH_GPU_EINVAL, "null argument");
+  if (!c->uploaded) return fail(GIRIH_GPU_ESTATE, "norms before upload");
+  DeviceGuard dg(c->d.device);
+  size_t n = host_array_elems(c);
+  int e = ensure_staging(c, n * 8);
+  if (e) return e;
+  CK(cudaMemcpyAsync(c->staging, ref_U1, n * c->hsz, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemsetAsync(c->acc, 0, 32, c->st));
+  const void *a = c->f[c->iu1];
+  if (c->tsz == 8 && c->hsz == 8)
+    CK(launch_norms<double, double>(c->g, (const double *)a, (const double *)c->staging, c->g, nullptr, c->acc, c->st));
+  else if (c->tsz == 8)
+    CK(launch_norms<double, float>(c->g, (const double *)a, (const float *)c->staging, c->g, nullptr, c->acc, c->st));
+  else if (c->hsz == 8)
+    CK(launch_norms<float, double>(c->g, (const float *)a, (const double *)c->staging, c->g, nullptr, c->acc, c->st));
+  else
+    CK(launch_norms<float, float>(c->g, (const float *)a, (const float *)c->staging, c->g, nullptr, c->acc, c->st));
+  return read_norms(c, out);
+}
+
+int girih_gpu_compare(girih_gpu_ctx *a, girih_gpu_ctx *b, double out[4]) {
+  if (!a || !b || !out) return fail(GIRIH_GPU_EINVAL, "null argument");
+  if (!a->uploaded || !b->uploaded) return fail(GIRIH_GPU_ESTATE, "compare before upload");
+  if (a->d.device != b->d.device || a->g.op != b->g.op || a->g.nx != b->g.nx || a->g.ny != b->g.ny ||
+      a->g.nz != b->g.nz)
+    return fail(GIRIH_GPU_EINVAL, "contexts differ in device, operator or grid");
+  DeviceGuard dg(a->d.device);
+  CK(cudaStreamSynchronize(b->st));
+  CK(cudaMemsetAsync(a->acc, 0, 32, a->st));
+  const void *pa = a->f[a->iu1], *pb = b->f[b->iu1];
+  if (a->tsz == 8 && b->tsz == 8)
+    CK(launch_norms<double, double>(a->g, (const double *)pa, nullptr, b->g, (const double *)pb, a->acc, a->st));
+  else if (a->tsz == 4 && b->tsz == 8)
+    CK(launch_norms<float, double>(a->g, (const float *)pa, nullptr, b->g, (const double *)pb, a->acc, a->st));
+  else if (a->tsz == 8)
+    CK(launch_norms<double, float>(a->g, (const double *)pa, nullptr, b->g, (const float *)pb, a->acc, a->st));
+  else
+    CK(launch_norms<float, float>(a->g, (const float *)pa, nullptr, b->g, (const float *)pb, a->acc, a->st));
+  return read_norms(a, out);
+}
+
+int girih_gpu_info(girih_gpu_ctx *c, girih_gpu_info_t *info) {
+  if (!c || !info) return fail(GIRIH_GPU_EINVAL, "null argument");
+  std::memset(info, 0, sizeof(*info));
+  const Geom &g = c->g;
+  info->precision = c->d.precision;
+  info->schedule = c->sched;
+  info->fusion_depth = c->sched == GIRIH_SCHED_FUSED ? c->fcfg.depth : 1;
+  info->block_x = c->sched == GIRIH_SCHED_FUSED ? c->fcfg.bx : 0;
+  info->block_y = c->sched == GIRIH_SCHED_FUSED ? c->fcfg.by : 0;
+  info->launches_last_run = c->last_launches;
+  info->steps_last_run = c->last_steps;
+  // compulsory traffic of one step: read v (+ u, roc2 for time order 2, + coefficient
+  // arrays), write u
+  double fb = c->tsz, cb = c->bf16coef ? 2.0 : c->tsz;
+  double bytes = 2 * fb;
+  if (g.to == 2) bytes += 2 * fb;
+  if (g.var) bytes += g.nc * cb;
+  info->bytes_per_lup = bytes;
+  info->device_bytes = c->dev_bytes;
+  std::snprintf(info->kernel_name, sizeof(info->kernel_name), "%s",
+                c->sched == GIRIH_SCHED_FUSED ? fused_kernel_name() : plain_kernel_name(g.op));
+  return 0;
+}
+
+}  // extern "C"

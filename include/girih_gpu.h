@@ -1,0 +1,152 @@
+/*
+ * libgirih_gpu -- GB300 (sm_103a) star-stencil time stepper behind a C ABI.
+ *
+ * This is the device boundary of the girih stencil hot path.  The reference
+ * plugs time steppers into a table of `void (*)(Parameters *)`
+ * (src/data_structures.h:412-415, table src/wrappers.h:28-36) and calls them
+ * from the performance harness (src/performance.c:75) and the verifier
+ * (src/verification.c:37).  A GPU stepper added to that table calls the entry
+ * points below; girih_gb300/host/gpu_ts.c is that stepper.
+ *
+ * Conventions
+ *   - every call returns 0 on success or a GIRIH_GPU_E* code; nothing aborts
+ *     (the reference's RAISE_ERROR, src/data_structures.h:417-432, exits);
+ *     girih_gpu_strerror() names a code, girih_gpu_last_error() gives detail;
+ *   - host arrays stay owned by the caller, in the reference layout: x-fastest
+ *     (src/kernels/stencils.h:29-32), shape ldomain_shape (interior + 2r halo,
+ *     x padded, src/utils.c:367-374), element size host_real_size (real_t);
+ *   - the library owns all device memory and copies in and out;
+ *   - one context = one grid on one device with one stream; contexts are not
+ *     thread-safe, distinct contexts may be used from distinct threads.
+ *
+ * Operator ids are the reference's --target-kernel ids
+ * (src/kernels/stencils.c:260-271) plus GIRIH_OP_STAR7_LEAPFROG:
+ *   0  star r=4, time order 2, constant coef (iso_ref, stencils.c:27-41)
+ *   1  star r=1, time order 1, constant coef (iso_ref_2space_1time, :73-78)
+ *   2  star r=1, variable coef, 2 arrays     (iso_ref_2space_1time_var, :94-99)
+ *   3  star r=1, variable axis-symmetric, 4  (..._var_axsym, :121-126)
+ *   4  star r=4, variable axis-symmetric, 13 (iso_ref_8space_1time_var_axsym, :148-162)
+ *   5  star r=1, variable no-symmetry, 7     (..._var_nosym, :193-201)
+ *   8  star r=1, time order 2, constant coef (radius-1 analogue of 0; no reference id)
+ */
+#ifndef GIRIH_GPU_H
+#define GIRIH_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GIRIH_GPU_ABI_VERSION 1
+
+enum {
+  GIRIH_GPU_OK = 0,
+  GIRIH_GPU_EINVAL = 1,       /* bad argument or inconsistent shapes */
+  GIRIH_GPU_EUNSUPPORTED = 2, /* operator / precision / schedule combination not provided */
+  GIRIH_GPU_ECUDA = 3,        /* a CUDA runtime call failed */
+  GIRIH_GPU_ENOMEM = 4,       /* device allocation failed */
+  GIRIH_GPU_ESTATE = 5,       /* call out of order (e.g. run before upload) */
+  GIRIH_GPU_ETIMEOUT = 6,     /* a bounded device-side wait gave up */
+  GIRIH_GPU_ENODEV = 7        /* no usable CUDA device */
+};
+
+enum { GIRIH_OP_STAR7_LEAPFROG = 8 };
+
+enum {
+  GIRIH_FP64 = 0,  /* FP64 fields and coefficients, FP64 arithmetic */
+  GIRIH_FP32 = 1,  /* FP32 fields and coefficients, FP32 arithmetic */
+  GIRIH_MIXED = 2  /* FP32 fields; variable coefficients in BF16 with a per-array
+                      FP32 scale; FP32 accumulation; compensated leapfrog update */
+};
+
+enum {
+  GIRIH_SCHED_PLAIN = 0, /* one time step per kernel launch */
+  GIRIH_SCHED_FUSED = 1, /* several time steps per HBM pass (temporal blocking) */
+  GIRIH_SCHED_AUTO = 2   /* fused where provided and profitable, else plain */
+};
+
+typedef struct {
+  int target_kernel;     /* operator id, see above */
+  int stencil_shape[3];  /* interior nx, ny, nz (Parameters.lstencil_shape) */
+  int ldomain_shape[3];  /* host array shape (Parameters.ldomain_shape) */
+  int host_real_size;    /* sizeof(real_t) of the host arrays: 8 or 4 */
+  int precision;         /* GIRIH_FP64 / GIRIH_FP32 / GIRIH_MIXED */
+  int schedule;          /* GIRIH_SCHED_* */
+  int fusion_depth;      /* time steps per pass for the fused schedule; 0 = autotune */
+  int block_x, block_y;  /* fused output tile; 0 = autotune */
+  int exact;             /* FP64 plain only: 1 = same rounding as the serial reference
+                            (no fused multiply-add, reference evaluation order) */
+  int device;            /* CUDA device ordinal */
+} girih_gpu_desc;
+
+typedef struct {
+  int precision, schedule;     /* what run() executes */
+  int fusion_depth;            /* time steps per launch (1 for plain) */
+  int block_x, block_y;        /* output tile of the fused kernel (0 for plain) */
+  int launches_last_run;       /* kernel launches issued by the last run() */
+  int steps_last_run;          /* time steps advanced by the last run() */
+  double bytes_per_lup;        /* compulsory HBM bytes per lattice update, one step per pass */
+  double device_bytes;         /* device memory held by the context */
+  char kernel_name[64];        /* dominant kernel of run() */
+} girih_gpu_info_t;
+
+typedef struct girih_gpu_ctx girih_gpu_ctx;
+
+/* Context lifetime.  create() validates the descriptor and allocates device
+ * memory; nothing is copied yet.  Replaces the reference's per-run
+ * arrays_allocate (src/utils.c:153-218) on the device side. */
+int girih_gpu_create(girih_gpu_ctx **out, const girih_gpu_desc *d);
+void girih_gpu_destroy(girih_gpu_ctx *c);
+
+/* Copy the caller's arrays (reference layout) to the device.  U3 (roc2) is
+ * required for time-order-2 operators and ignored otherwise; coef holds r+1
+ * scalars for constant operators and n arrays of ldomain size otherwise
+ * (COEF macro, src/kernels/stencils.h:32). */
+int girih_gpu_upload(girih_gpu_ctx *c, const void *U1, const void *U2, const void *U3,
+                     const void *coef);
+
+/* Advance the grid like the reference's steppers: for it in 0..nt step 2
+ * { U1 <- op(U2); U2 <- op(U1) } (src/kernels/nb_naive_ts.c:187-203), so odd nt
+ * runs nt+1 steps.  Continues from the current device state.  *ms_out (may be
+ * NULL) receives the device time of the whole loop from CUDA events on the
+ * context's stream; the loop is replayed from a captured CUDA graph. */
+int girih_gpu_run(girih_gpu_ctx *c, int nt, float *ms_out);
+
+/* Copy the current U1 (state after steps-1 updates) and U2 (after all steps)
+ * back into the caller's arrays (halo included, padding untouched); either
+ * pointer may be NULL. */
+int girih_gpu_download(girih_gpu_ctx *c, void *U1, void *U2);
+
+/* FP64 device reduction of the current U1 against a reference U1 given in the
+ * host layout: out = {max|a-b|, max|b|, sum (a-b)^2, sum b^2} over the
+ * interior.  max-norm relative error = out[0]/out[1]. */
+int girih_gpu_error_norms(girih_gpu_ctx *c, const void *ref_U1, double out[4]);
+
+/* The same norms between the U1 of two contexts on the same device and grid
+ * (a = test, b = reference), without leaving the device. */
+int girih_gpu_compare(girih_gpu_ctx *a, girih_gpu_ctx *b, double out[4]);
+
+/* Seeded synthetic initialisation on the device, bit-identical to the CPU
+ * oracle's go_fill_seeded(): ranges = {f_lo, f_hi, roc2_lo, roc2_hi, c_lo,
+ * c_hi}; const_coefs gives the r+1 scalars of a constant operator.  With
+ * GIRIH_SEED_F32_EXACT in flags every value is first rounded to FP32, so FP32
+ * and FP64 contexts start from identical data. */
+enum { GIRIH_SEED_F32_EXACT = 1 };
+int girih_gpu_fill_seeded(girih_gpu_ctx *c, uint64_t seed, const double ranges[6],
+                          const double *const_coefs, int flags);
+
+/* Copy the device roc2 array (time-order-2 operators, Parameters.U3) back into
+ * the caller's array in the reference layout. */
+int girih_gpu_download_roc2(girih_gpu_ctx *c, void *U3);
+
+int girih_gpu_info(girih_gpu_ctx *c, girih_gpu_info_t *info);
+
+const char *girih_gpu_strerror(int err);
+const char *girih_gpu_last_error(void); /* detail of the calling thread's last error */
+int girih_gpu_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -124,26 +124,36 @@ double go_seeded_value(uint64_t seed, uint32_t stream, uint64_t idx, double lo, 
   return lo + m;
 }
 
+static double seeded_maybe_f32(uint64_t seed, uint32_t stream, uint64_t idx, double lo, double hi,
+                               int round_f32) {
+  double v = go_seeded_value(seed, stream, idx, lo, hi);
+  return round_f32 ? (double)(float)v : v;
+}
+
 void go_fill_seeded(int op, int nx, int ny, int nz, int pnx, uint64_t seed, double f_lo,
                     double f_hi, double r_lo, double r_hi, double c_lo, double c_hi, double *U1,
-                    double *U2, double *U3, double *coef) {
+                    double *U2, double *U3, double *coef, int round_f32, int nthreads) {
   int r, to, nc, arr;
   if (go_op_info(op, &r, &to, &nc, &arr)) return;
   const int64_t nnx = nx + 2 * r, nny = ny + 2 * r, nnz = nz + 2 * r;
   const int64_t ln = (int64_t)pnx * nny * nnz;
+  int nth = nthreads < 1 ? 1 : nthreads;
+  (void)nth;
+#pragma omp parallel for num_threads(nth) if (nth > 1) schedule(static)
   for (int64_t k = 0; k < nnz; k++)
     for (int64_t j = 0; j < nny; j++)
       for (int64_t i = 0; i < pnx; i++) {
         int64_t idx = (k * nny + j) * pnx + i;
         int in = i < nnx;
         uint64_t g = (uint64_t)((k * nny + j) * nnx + i);
-        double f = in ? go_seeded_value(seed, 0, g, f_lo, f_hi) : 0.0;
+        double f = in ? seeded_maybe_f32(seed, 0, g, f_lo, f_hi, round_f32) : 0.0;
         U1[idx] = f;
         U2[idx] = f;
-        if (to == 2 && U3) U3[idx] = in ? go_seeded_value(seed, 1, g, r_lo, r_hi) : 0.0;
+        if (to == 2 && U3) U3[idx] = in ? seeded_maybe_f32(seed, 1, g, r_lo, r_hi, round_f32) : 0.0;
         if (arr && coef)
           for (int m = 0; m < nc; m++)
-            coef[idx + m * ln] = in ? go_seeded_value(seed, 2 + (uint32_t)m, g, c_lo, c_hi) : 0.0;
+            coef[idx + m * ln] =
+                in ? seeded_maybe_f32(seed, 2 + (uint32_t)m, g, c_lo, c_hi, round_f32) : 0.0;
       }
 }
 

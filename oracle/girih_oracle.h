@@ -64,11 +64,14 @@ double go_seeded_value(uint64_t seed, uint32_t stream, uint64_t idx, double lo, 
  * halo included, gets a value indexed by its unpadded linear index; padding
  * columns are zero.  U1 and U2 get identical field values (stream 0), U3 gets
  * roc2 values (stream 1, [r_lo, r_hi)), variable coefficient array m gets
- * stream 2+m in [c_lo, c_hi).  Constant-coefficient scalars are not touched. */
+ * stream 2+m in [c_lo, c_hi).  Constant-coefficient scalars are not touched.
+ * round_f32 != 0 rounds every value to the nearest FP32 number (kept as double),
+ * so FP32 and FP64 runs can start from identical data.  nthreads > 1 fills
+ * with OpenMP; the values do not depend on it. */
 void go_fill_seeded(int op, int nx, int ny, int nz, int pnx, uint64_t seed,
                     double f_lo, double f_hi, double r_lo, double r_hi,
                     double c_lo, double c_hi,
-                    double *U1, double *U2, double *U3, double *coef);
+                    double *U1, double *U2, double *U3, double *coef, int round_f32, int nthreads);
 
 /* One sweep u <- op(v) over the interior, in the reference's evaluation order
  * (src/verification.c:315-479, 786-819).  Halo and padding are never written.

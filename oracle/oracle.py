@@ -46,7 +46,7 @@ def lib():
         d = ctypes.POINTER(ctypes.c_double)
         i = ctypes.c_int
         L.go_fill_ref.argtypes = [i, i, i, i, i, d, d, d, d]
-        L.go_fill_seeded.argtypes = [i, i, i, i, i, ctypes.c_uint64] + [ctypes.c_double] * 6 + [d] * 4
+        L.go_fill_seeded.argtypes = [i, i, i, i, i, ctypes.c_uint64] + [ctypes.c_double] * 6 + [d] * 4 + [i, i]
         L.go_step.argtypes = [i, i, i, i, i, d, d, d, d, i]
         L.go_run.argtypes = [i, i, i, i, i, i, d, d, d, d, i]
         L.go_norms.argtypes = [d, d, i, i, i, i, i, d]
@@ -95,11 +95,12 @@ class Grid:
                           _p(self.U1), _p(self.U2), _p(self.U3), _p(self.coef))
         return self
 
-    def fill_seeded(self, seed, f=(0.0, 1.0), roc2=(0.0, 0.0), c=(0.0, 0.0), coefs=None):
+    def fill_seeded(self, seed, f=(0.0, 1.0), roc2=(0.0, 0.0), c=(0.0, 0.0), coefs=None, f32_exact=False,
+                    nthreads=1):
         lib().go_fill_seeded(self.op, self.nx, self.ny, self.nz, self.pnx, seed,
                              f[0], f[1], roc2[0], roc2[1], c[0], c[1],
                              _p(self.U1), _p(self.U2), _p(self.U3),
-                             _p(self.coef) if self.coef_arrays else None)
+                             _p(self.coef) if self.coef_arrays else None, 1 if f32_exact else 0, nthreads)
         if coefs is not None and not self.coef_arrays:
             self.coef[:len(coefs)] = coefs
         return self

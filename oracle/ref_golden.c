@@ -89,7 +89,7 @@ int main(int argc, char **argv) {
     if (go_op_info(op, &r, &to, &nc, &arr)) return 3;
     go_fill_seeded(op, p.stencil_shape[0], p.stencil_shape[1], p.stencil_shape[2],
                    p.ldomain_shape[0], seed, v[0], v[1], v[2], v[3], v[4], v[5], p.U1, p.U2,
-                   p.U3, p.coef);
+                   p.U3, p.coef, 0, 1);
     if (!arr)
       for (int i = 0; i < nc && 16 + i < argc; i++) p.coef[i] = atof(argv[16 + i]);
   } else if (strcmp(mode, "ref") != 0) {

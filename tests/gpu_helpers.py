@@ -1,0 +1,45 @@
+"""Shared helpers for the GPU parity tests: build oracle grids and GPU contexts
+from the same seeded or reference inputs."""
+import numpy as np
+
+import oracle
+from girih_gb300 import gpu
+
+# standard 8th-order second-difference weights over 3 axes (sum 0), rounded to
+# FP32-representable values so FP32 and FP64 runs share one operator
+LAP8 = [float(np.float32(x)) for x in (3 * (-205.0 / 72.0), 8.0 / 5.0, -1.0 / 5.0, 8.0 / 315.0, -1.0 / 560.0)]
+LAP2 = [-0.75, 0.125]  # 7-point Laplacian weights (c0 = -6 c1), FP32-representable
+
+SEED_PARAMS = {  # op -> (f range, roc2 range, coef range, constant coefs)
+    0: ((-1.0, 1.0), (0.05, 0.15), (0.0, 0.0), LAP8),
+    1: ((0.0, 1.0), (0.0, 0.0), (0.0, 0.0), None),  # reference default coefficients
+    2: ((0.0, 1.0), (0.0, 0.0), (0.01, 0.1), None),
+    3: ((0.0, 1.0), (0.0, 0.0), (0.01, 0.1), None),
+    4: ((0.0, 1.0), (0.0, 0.0), (0.01, 0.025), None),
+    5: ((0.0, 1.0), (0.0, 0.0), (0.01, 0.1), None),
+    8: ((0.0, 1.0), (0.5, 1.5), (0.0, 0.0), LAP2),
+}
+
+
+def oracle_grid(op, nx, ny, nz, seed=None):
+    """Oracle grid with seeded inputs (seed given) or the reference's own init."""
+    g = oracle.Grid(op, nx, ny, nz)
+    if seed is None:
+        g.fill_ref()
+        return g
+    f, r2, c, coefs = SEED_PARAMS[op]
+    g.fill_seeded(seed, f, r2, c, coefs=coefs)
+    if not g.coef_arrays and coefs is None:
+        g.coef[:] = g.default_coefs()
+    return g
+
+
+def gpu_context(g, **kw):
+    ctx = gpu.Context(g.op, g.nx, g.ny, g.nz, pnx=g.pnx, **kw)
+    ctx.upload(g.U1, g.U2, g.U3, g.coef)
+    return ctx
+
+
+def max_rel(a, b, g):
+    n = oracle.norms(a, b, g)
+    return n[0] / n[1] if n[1] > 0 else n[0]

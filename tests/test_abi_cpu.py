@@ -1,0 +1,73 @@
+"""CPU-side checks of the C ABI: the library builds, loads, and exports every
+entry point include/girih_gpu.h declares; without a GPU, create() reports
+ENODEV instead of crashing.  No compute calls are made here."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from girih_gb300 import gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADERS = [os.path.join(ROOT, "include", f) for f in sorted(os.listdir(os.path.join(ROOT, "include")))
+           if f.endswith(".h")]
+
+
+def declared_symbols():
+    names = set()
+    for h in HEADERS:
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(girih_\w+)\s*\(", text, flags=re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_headers_declare_entry_points():
+    names = declared_symbols()
+    for must in ("girih_gpu_create", "girih_gpu_upload", "girih_gpu_run", "girih_gpu_download",
+                 "girih_gpu_error_norms", "girih_gpu_destroy", "girih_gpu_strerror"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = gpu.lib()
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+    out = subprocess.run(["nm", "-D", "--defined-only", gpu.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (girih_\w+)", out))
+    assert set(declared_symbols()) <= exported
+
+
+def test_abi_version_and_strerror():
+    lib = gpu.lib()
+    assert lib.girih_gpu_abi_version() == 1
+    for code in range(0, 8):
+        assert lib.girih_gpu_strerror(code)
+    assert lib.girih_gpu_strerror(99) == b"unknown error"
+
+
+def test_create_validates_before_touching_the_device():
+    with pytest.raises(gpu.GirihGpuError) as e:
+        gpu.Context(6, 8, 8, 8)  # solar operator: not a star operator on the GPU
+    assert e.value.code == 2
+    with pytest.raises(gpu.GirihGpuError) as e:
+        gpu.Context(1, 8, 8, 8, pnx=5)  # pitch smaller than nx + 2r
+    assert e.value.code == 1
+
+
+def test_null_arguments_are_rejected():
+    lib = gpu.lib()
+    assert lib.girih_gpu_create(None, None) == 1
+    assert lib.girih_gpu_run(None, 2, None) == 1
+    assert lib.girih_gpu_upload(None, None, None, None, None) == 1
+    lib.girih_gpu_destroy(None)  # no-op
+
+
+@pytest.mark.skipif(__import__("torch").cuda.is_available(), reason="checks the no-GPU path")
+def test_no_device_is_an_error_code():
+    with pytest.raises(gpu.GirihGpuError) as e:
+        gpu.Context(1, 8, 8, 8)
+    assert e.value.code == 7

@@ -1,0 +1,123 @@
+"""Parity of the time-fused (temporally blocked) GPU kernels with the oracle.
+
+FP64 fused passes use FMA contraction, so they are held to the FP64 parity
+bound (max-norm relative <= 1e-12) rather than bit equality.  Every fusion
+depth and both tile variants are exercised on grids that are not multiples of
+the tile, with odd nt (the reference rounds nt up to even) and with nt not a
+multiple of the depth (a shorter final pass).
+"""
+import numpy as np
+import pytest
+
+from girih_gb300 import gpu
+from gpu_helpers import gpu_context, max_rel, oracle_grid
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+FUSED_OPS = [1, 8, 0]
+MAX_DEPTH = {("fp64", 1): 4, ("fp64", 4): 2, ("fp32", 1): 6, ("fp32", 4): 2, ("mixed", 1): 6, ("mixed", 4): 2}
+TILE = {0: (64, 32), 1: (32, 64)}  # column region of the two CTA variants
+
+
+def _block(op, depth, variant):
+    r = gpu.OP_INFO[op][0]
+    w, h = TILE[variant]
+    return (w - 2 * depth * r, h - 2 * depth * r)
+
+
+def _shape(op):
+    return (70, 53, 41) if gpu.OP_INFO[op][0] == 1 else (61, 37, 29)
+
+
+@pytest.mark.parametrize("op", FUSED_OPS)
+@pytest.mark.parametrize("variant", [0, 1])
+def test_fused_fp64_all_depths(op, variant):
+    r = gpu.OP_INFO[op][0]
+    g0 = oracle_grid(op, *_shape(op), seed=7)
+    nt = 9
+    ref = g0.copy().run(nt, nthreads=4)
+    for depth in range(1, MAX_DEPTH[("fp64", r)] + 1):
+        g = g0.copy()
+        with gpu_context(g, precision="fp64", schedule="fused", fusion_depth=depth,
+                         block=_block(op, depth, variant)) as ctx:
+            info = ctx.info()
+            assert info["schedule"] == gpu.FUSED and info["fusion_depth"] == depth
+            ctx.run(nt)
+            assert ctx.info()["launches_last_run"] == -(-10 // depth)
+            u1, u2 = ctx.download()
+        assert max_rel(u1, ref.U1, ref) <= FP64_TOL, (depth, max_rel(u1, ref.U1, ref))
+        assert max_rel(u2, ref.U2, ref) <= FP64_TOL, depth
+        # halos and padding are never written
+        np.testing.assert_array_equal(u1[:, :, g.nx + 2 * r:], g0.U1[:, :, g.nx + 2 * r:])
+        np.testing.assert_array_equal(u1[:r], g0.U1[:r])
+
+
+@pytest.mark.parametrize("op", FUSED_OPS)
+@pytest.mark.parametrize("precision", ["fp32", "mixed"])
+def test_fused_fp32_against_fp64_oracle(op, precision):
+    r = gpu.OP_INFO[op][0]
+    g0 = oracle_grid(op, *_shape(op), seed=8)
+    nt = 12
+    ref = g0.copy().run(nt, nthreads=4)
+    with gpu_context(g0.copy(), precision="fp32", schedule="plain") as pc:
+        pc.run(nt)
+        plain_u1, _ = pc.download()
+    plain_err = max_rel(plain_u1, ref.U1, ref)
+    for depth in range(1, MAX_DEPTH[(precision, r)] + 1):
+        with gpu_context(g0.copy(), precision=precision, schedule="fused", fusion_depth=depth) as ctx:
+            ctx.run(nt)
+            u1, _ = ctx.download()
+        err = max_rel(u1, ref.U1, ref)
+        # same order of error as the plain FP32 kernel (inputs are FP32-representable)
+        assert err < max(4 * plain_err, 2e-6), (depth, err, plain_err)
+
+
+@pytest.mark.parametrize("op", FUSED_OPS)
+@pytest.mark.parametrize("shape", [(1, 1, 1), (3, 70, 2), (90, 2, 9), (64, 32, 5)])
+def test_fused_edge_shapes(op, shape):
+    g0 = oracle_grid(op, *shape, seed=9)
+    nt = 5
+    ref = g0.copy().run(nt)
+    r = gpu.OP_INFO[op][0]
+    for depth in (1, MAX_DEPTH[("fp64", r)]):
+        with gpu_context(g0.copy(), precision="fp64", schedule="fused", fusion_depth=depth) as ctx:
+            ctx.run(nt)
+            u1, u2 = ctx.download()
+        assert max_rel(u1, ref.U1, ref) <= FP64_TOL
+        assert max_rel(u2, ref.U2, ref) <= FP64_TOL
+
+
+def test_fused_reference_init_and_nt0():
+    g0 = oracle_grid(1, 40, 30, 20)  # reference ramp + boundary sources
+    with gpu_context(g0.copy(), schedule="fused", fusion_depth=3) as ctx:
+        ctx.run(0)
+        u1, u2 = ctx.download()
+        np.testing.assert_array_equal(u1, g0.U1)
+        ctx.run(8)
+        ctx.run(6)
+        u1, u2 = ctx.download()
+    ref = g0.copy().run(14)
+    assert max_rel(u1, ref.U1, ref) <= FP64_TOL
+    assert max_rel(u2, ref.U2, ref) <= FP64_TOL
+
+
+def test_fused_requires_equal_halos():
+    g = oracle_grid(8, 20, 20, 20, seed=1)
+    g.U1[0, 0, 0] += 1.0  # U1 halo differs from U2's
+    ctx = gpu.Context(8, 20, 20, 20, schedule="fused")
+    with pytest.raises(gpu.GirihGpuError) as e:
+        ctx.upload(g.U1, g.U2, g.U3, g.coef)
+    assert e.value.code == 2
+    ctx.close()
+    # the plain schedule keeps the exact ping-pong semantics for unequal halos
+    with gpu_context(g.copy(), schedule="plain", exact=True) as ctx:
+        ctx.run(4)
+        u1, _ = ctx.download()
+    np.testing.assert_array_equal(u1, g.copy().run(4).U1)
+
+
+def test_auto_schedule_picks_fused_where_provided():
+    for op, want in ((1, gpu.FUSED), (8, gpu.FUSED), (0, gpu.FUSED), (5, gpu.PLAIN)):
+        with gpu.Context(op, 32, 32, 32, schedule="auto") as ctx:
+            assert ctx.info()["schedule"] == want

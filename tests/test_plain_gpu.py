@@ -1,0 +1,166 @@
+"""Parity of the plain (one step per launch) GPU kernels with the reference.
+
+Bit-exact for the FP64 `exact` mode against the golden vectors produced by the
+reference itself; max-norm relative error <= 1e-12 for the fast FP64 mode; FP32
+and mixed forms against the FP64 oracle with the tolerances stated per test.
+All calls go through the C ABI (girih_gb300.gpu binds libgirih_gpu.so).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from girih_gb300 import gpu
+from gpu_helpers import gpu_context, max_rel, oracle_grid
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "golden_ref.npz")
+_data = np.load(GOLD)
+SPECS = json.loads(bytes(_data["specs"]).decode())
+GPU_CASES = sorted(n for n, s in SPECS.items() if s["op"] in gpu.OP_INFO)
+
+FP64_TOL = 1e-12  # max-norm relative, FP64 plain against the serial reference
+
+
+def _golden_grid(name):
+    s = SPECS[name]
+    g = oracle.Grid(s["op"], s["nx"], s["ny"], s["nz"])
+    if s["init"] == "ref":
+        g.fill_ref()
+    else:
+        sp = s["seeded"]
+        g.fill_seeded(sp["seed"], tuple(sp["f"]), tuple(sp["roc2"]), tuple(sp["c"]), coefs=sp.get("coefs"))
+        if not g.coef_arrays and not sp.get("coefs"):
+            g.coef[:] = g.default_coefs()
+    return g, s
+
+
+@pytest.mark.parametrize("name", GPU_CASES)
+def test_exact_fp64_is_bit_identical_to_reference(name):
+    g, s = _golden_grid(name)
+    with gpu_context(g, precision="fp64", schedule="plain", exact=True) as ctx:
+        ctx.run(s["nt"])
+        u1, u2 = ctx.download()
+    np.testing.assert_array_equal(g.interior(u1), g.interior(_data[name + "__U1"]))
+    np.testing.assert_array_equal(u1, _data[name + "__U1"])
+    np.testing.assert_array_equal(u2, _data[name + "__U2"])
+
+
+@pytest.mark.parametrize("name", GPU_CASES)
+def test_fast_fp64_within_1e12(name):
+    g, s = _golden_grid(name)
+    with gpu_context(g, precision="fp64", schedule="plain") as ctx:
+        ctx.run(s["nt"])
+        u1, u2 = ctx.download()
+        dev = gpu.rel_errors(ctx.error_norms(_data[name + "__U1"]))[0]
+    assert max_rel(u1, _data[name + "__U1"], g) <= FP64_TOL
+    assert max_rel(u2, _data[name + "__U2"], g) <= FP64_TOL
+    assert dev <= FP64_TOL
+
+
+@pytest.mark.parametrize("op", sorted(gpu.OP_INFO))
+@pytest.mark.parametrize("shape", [(67, 45, 39), (33, 9, 70), (1, 1, 1), (130, 3, 2)])
+def test_plain_fp64_seeded_against_oracle(op, shape):
+    nt = 7  # odd: the reference runs 8 sweeps
+    g = oracle_grid(op, *shape, seed=11)
+    with gpu_context(g, precision="fp64", exact=True) as ctx:
+        ctx.run(nt)
+        u1, u2 = ctx.download()
+    g.run(nt, nthreads=4)
+    np.testing.assert_array_equal(u1, g.U1)
+    np.testing.assert_array_equal(u2, g.U2)
+
+
+@pytest.mark.parametrize("op", sorted(gpu.OP_INFO))
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_device_seeded_init_matches_oracle(op, precision):
+    g = oracle_grid(op, 21, 13, 11, seed=5)
+    f, r2, c, coefs = __import__("gpu_helpers").SEED_PARAMS[op]
+    with gpu.Context(op, 21, 13, 11, precision=precision) as ctx:
+        ctx.fill_seeded(5, f, r2, c, coefs=coefs if coefs is not None else list(g.coef[:5]))
+        u1, u2 = ctx.download()
+    want = g.U1 if precision == "fp64" else g.U1.astype(np.float32).astype(np.float64)
+    np.testing.assert_array_equal(u1, want)
+    np.testing.assert_array_equal(u2, want)
+
+
+@pytest.mark.parametrize("op", sorted(gpu.OP_INFO))
+def test_plain_fp32_against_fp64_oracle(op):
+    nt = 10
+    g = oracle_grid(op, 40, 24, 20, seed=3)
+    with gpu_context(g, precision="fp32") as ctx:
+        ctx.run(nt)
+        u1, _ = ctx.download()
+    g.run(nt, nthreads=4)
+    err = max_rel(u1, g.U1, g)
+    assert err < 5e-6, err  # FP32 storage and arithmetic over 10 steps
+
+
+@pytest.mark.parametrize("op", [2, 3, 4, 5])
+def test_mixed_bf16_coefficients_error_is_bounded(op):
+    """BF16 coefficient arrays carry a 2^-9 relative quantisation error; the
+    error against the FP64 oracle is reported, and bounded here by 1e-2."""
+    nt = 10
+    g = oracle_grid(op, 40, 24, 20, seed=3)
+    with gpu_context(g, precision="mixed") as ctx:
+        ctx.run(nt)
+        u1, _ = ctx.download()
+        assert ctx.info()["bytes_per_lup"] == 8 + 2 * gpu.OP_INFO[op][2]
+    g.run(nt, nthreads=4)
+    err = max_rel(u1, g.U1, g)
+    assert 0 < err < 1e-2, err
+
+
+def test_run_continues_from_state():
+    g = oracle_grid(1, 30, 20, 10, seed=2)
+    with gpu_context(g, exact=True) as ctx:
+        ctx.run(4)
+        ctx.run(6)
+        u1, u2 = ctx.download()
+    g.run(10)
+    np.testing.assert_array_equal(u1, g.U1)
+    np.testing.assert_array_equal(u2, g.U2)
+
+
+def test_float_host_arrays():
+    """Host arrays of a single-precision reference build (real_t = float)."""
+    g = oracle_grid(1, 30, 20, 10, seed=2)
+    ctx = gpu.Context(1, 30, 20, 10, precision="fp32", host_real_size=4)
+    f32 = lambda a: a.astype(np.float32)
+    ctx.upload(f32(g.U1), f32(g.U2), None, f32(g.coef))
+    ctx.run(4)
+    u1, _ = ctx.download()
+    assert u1.dtype == np.float32
+    g.run(4)
+    assert max_rel(u1.astype(np.float64), g.U1, g) < 1e-5
+    ctx.close()
+
+
+def test_error_codes():
+    with pytest.raises(gpu.GirihGpuError) as e:
+        gpu.Context(7, 8, 8, 8)  # box operator: not provided on the GPU
+    assert e.value.code == 2
+    with pytest.raises(gpu.GirihGpuError) as e:
+        gpu.Context(1, 0, 8, 8)
+    assert e.value.code == 1
+    ctx = gpu.Context(1, 8, 8, 8)
+    with pytest.raises(gpu.GirihGpuError) as e:
+        ctx.run(2)  # before upload
+    assert e.value.code == 5
+    with pytest.raises(gpu.GirihGpuError) as e:
+        gpu.Context(1, 8, 8, 8, schedule="fused", exact=True)
+    assert e.value.code == 2
+    ctx.close()
+
+
+def test_non_finite_result_is_visible_in_norms():
+    g = oracle_grid(1, 16, 16, 16, seed=1)
+    bad = g.U1.copy()
+    with gpu_context(g) as ctx:
+        ctx.run(0)
+        bad[5, 5, 5] = np.nan
+        n = ctx.error_norms(bad)
+    assert np.isnan(n[1]) or np.isnan(n[0])

@@ -80,7 +80,11 @@ def test_device_seeded_init_matches_oracle(op, precision):
     g = oracle_grid(op, 21, 13, 11, seed=5)
     f, r2, c, coefs = __import__("gpu_helpers").SEED_PARAMS[op]
     with gpu.Context(op, 21, 13, 11, precision=precision) as ctx:
-        ctx.fill_seeded(5, f, r2, c, coefs=coefs if coefs is not None else list(g.coef[:5]))
+        if g.coef_arrays:
+            coefs = None
+        elif coefs is None:
+            coefs = list(g.coef[:5])
+        ctx.fill_seeded(5, f, r2, c, coefs=coefs)
         u1, u2 = ctx.download()
     want = g.U1 if precision == "fp64" else g.U1.astype(np.float32).astype(np.float64)
     np.testing.assert_array_equal(u1, want)

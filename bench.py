@@ -258,6 +258,7 @@ def run_ours(args, wl, rank, world, local):
         "ms_per_step": h["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if h["precision"] != "fp64" else "f64", "data": "synthetic (seeded SplitMix64, FP32-representable)",
         "config": {"workload": WORKLOAD_NAME, "operator": op, "grid": [n, n, n], "nt": nt, "headline_form": head,
+                   "fusion_depth": h["depth"], "tile": h["tile"],
                    "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (no flush needed)"},
         "forms": {k: {kk: v[kk] for kk in ("glups", "ms_per_step", "launches_per_step", "depth", "tile")}
                   for k, v in results.items()},
@@ -336,13 +337,19 @@ def main():
     ap.add_argument("--forms", default="")
     ap.add_argument("--headline", default="mixed")
     ap.add_argument("--depth", type=int, default=0)
+    ap.add_argument("--n", type=int, default=0, help="override the grid edge (small profiling cases)")
+    ap.add_argument("--nt", type=int, default=0, help="override the number of time steps")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-error", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     WORKLOAD_NAME = args.workload
-    wl = WORKLOADS[args.workload]
+    wl = dict(WORKLOADS[args.workload])
+    if args.n:
+        wl["n"] = args.n
+    if args.nt:
+        wl["nt"] = args.nt
     rank, world, local = rank_env()
     if world > 1 and args.impl == "ours":
         import torch

@@ -1,0 +1,183 @@
+// Time-fused stepping for callers that cannot allocate device memory.
+//
+// girih_gpu_run() keeps two spare state buffers per context, allocated with
+// cudaMalloc when the context is created.  Some callers cannot do that: a host
+// application that owns the device's memory through its own pool (a cudaMalloc
+// behind its back escapes its accounting, or fails under its memory cap), or a
+// code path that must not take the implicit device synchronisation that
+// cudaMalloc/cudaFree can cause.  girih_gpu_fused_run_noalloc() serves them: the
+// caller passes its own device arrays, and the two spare buffers live in the
+// file-scope array below instead.
+//
+// The array is GIRIH_NOALLOC_SCRATCH_BYTES (64 MiB) of static device memory;
+// every GPU that loads this library holds it until the process exits.  All
+// calls share it and it keeps the last call's contents, so calls whose work
+// overlaps on the GPU (different streams, different host threads) race on it:
+// serialise them.  Each call re-initialises what it reads (both spare buffers
+// are overwritten from U2 before the first pass).
+#include <mutex>
+#include <string>
+
+#include "fused.cuh"
+#include "internal.cuh"
+
+namespace girih {
+namespace {
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[GIRIH_NOALLOC_SCRATCH_BYTES];
+
+constexpr size_t kFlagBytes = 256;  // halo-equality flag, then the two spare buffers
+constexpr int kMaxDevices = 64;
+
+std::mutex g_setup_mutex;
+void *g_scratch_addr[kMaxDevices] = {};
+
+// Device address of the scratch array on the current device, looked up once
+// per device.  In host code the array's name is only a host-side stand-in.
+int scratch_address(int dev, unsigned char **out) {
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
+  if (!g_scratch_addr[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      set_error(std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+      return GIRIH_GPU_ECUDA;
+    }
+    g_scratch_addr[dev] = p;
+  }
+  *out = static_cast<unsigned char *>(g_scratch_addr[dev]);
+  return 0;
+}
+
+// Geometry of arrays kept in the reference layout itself (x pitch ldomain_shape[0]).
+Geom reference_layout_geom(const girih_gpu_desc *d) {
+  Geom g{};
+  op_info(d->target_kernel, &g.r, &g.to, &g.nc, &g.var);
+  g.op = d->target_kernel;
+  g.nx = d->stencil_shape[0];
+  g.ny = d->stencil_shape[1];
+  g.nz = d->stencil_shape[2];
+  g.nnx = g.nx + 2 * g.r;
+  g.nny = g.ny + 2 * g.r;
+  g.nnz = g.nz + 2 * g.r;
+  g.hpx = d->ldomain_shape[0];
+  g.ox = 0;
+  g.px = d->ldomain_shape[0];
+  g.plane = (int64_t)g.px * g.nny;
+  g.elems = g.plane * g.nnz;
+  return g;
+}
+
+int fail_na(int code, const std::string &msg) {
+  set_error(msg);
+  return code;
+}
+
+#define NA_CK(...)                                                            \
+  do {                                                                        \
+    cudaError_t e_ = (__VA_ARGS__);                                           \
+    if (e_ != cudaSuccess) {                                                  \
+      set_error(std::string(#__VA_ARGS__) + ": " + cudaGetErrorString(e_));   \
+      return GIRIH_GPU_ECUDA;                                                 \
+    }                                                                         \
+  } while (0)
+
+}  // namespace
+}  // namespace girih
+
+using namespace girih;
+
+extern "C" int girih_gpu_fused_run_noalloc(const girih_gpu_desc *d, void *U1, void *U2, const void *U3,
+                                           const double *coefs, int nt, void *stream) {
+  if (!d || !U1 || !U2 || !coefs) return fail_na(GIRIH_GPU_EINVAL, "null argument");
+  int r, to, nc, var;
+  if (op_info(d->target_kernel, &r, &to, &nc, &var) || var)
+    return fail_na(GIRIH_GPU_EUNSUPPORTED, "no fused kernel for operator " + std::to_string(d->target_kernel));
+  const int nx = d->stencil_shape[0], ny = d->stencil_shape[1], nz = d->stencil_shape[2];
+  if (nx < 1 || ny < 1 || nz < 1 || d->ldomain_shape[0] < nx + 2 * r || d->ldomain_shape[1] != ny + 2 * r ||
+      d->ldomain_shape[2] != nz + 2 * r)
+    return fail_na(GIRIH_GPU_EINVAL, "ldomain_shape must be (>= nx+2r, ny+2r, nz+2r)");
+  if (d->precision < GIRIH_FP64 || d->precision > GIRIH_MIXED) return fail_na(GIRIH_GPU_EINVAL, "bad precision");
+  if (to == 2 && !U3) return fail_na(GIRIH_GPU_EINVAL, "time-order-2 operator needs U3 (roc2)");
+  if (nt < 0) return fail_na(GIRIH_GPU_EINVAL, "nt must be >= 0");
+  if (d->device < 0 || d->device >= kMaxDevices) return fail_na(GIRIH_GPU_EINVAL, "device ordinal out of range");
+
+  const int tsz = d->precision == GIRIH_FP64 ? 8 : 4;
+  const Geom g = reference_layout_geom(d);
+  const size_t state_bytes = (size_t)g.elems * tsz;
+  const size_t spare_bytes = (state_bytes + 255) / 256 * 256;
+  if (kFlagBytes + 2 * spare_bytes > (size_t)GIRIH_NOALLOC_SCRATCH_BYTES)
+    return fail_na(GIRIH_GPU_EINVAL,
+                   "grid too large for the no-allocation entry point: two state arrays of " +
+                       std::to_string(state_bytes) + " bytes exceed its " +
+                       std::to_string((unsigned long long)GIRIH_NOALLOC_SCRATCH_BYTES) + "-byte scratch");
+  FusedConfig cfg = choose_fused_config(g, d->precision, d->fusion_depth, d->block_x, d->block_y);
+  if (!cfg.depth) return fail_na(GIRIH_GPU_EUNSUPPORTED, "requested fused tile/depth is not provided");
+
+  int prev_dev = -1;
+  cudaGetDevice(&prev_dev);
+  if (prev_dev != d->device) NA_CK(cudaSetDevice(d->device));
+  struct Restore {
+    int dev;
+    ~Restore() {
+      int cur = -1;
+      cudaGetDevice(&cur);
+      if (dev >= 0 && cur != dev) cudaSetDevice(dev);
+    }
+  } restore{prev_dev};
+
+  unsigned char *scratch = nullptr;
+  int e = scratch_address(d->device, &scratch);
+  if (e) return e;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned int *flag = reinterpret_cast<unsigned int *>(scratch);
+  void *spare0 = scratch + kFlagBytes;
+  void *spare1 = scratch + kFlagBytes + spare_bytes;
+
+  // the fused schedule needs U1 and U2 to carry the same fixed halo
+  NA_CK(cudaMemsetAsync(flag, 0, sizeof(unsigned int), st));
+  NA_CK(launch_halo_equal(g, U1, U2, tsz, flag, st));
+  unsigned int h = 1;
+  NA_CK(cudaMemcpyAsync(&h, flag, sizeof(h), cudaMemcpyDeviceToHost, st));
+  NA_CK(cudaStreamSynchronize(st));
+  if (h != 0) return fail_na(GIRIH_GPU_EUNSUPPORTED, "U1 and U2 halos differ; the fused schedule needs them equal");
+
+  // spare buffers start as copies of U2 so that their halos hold the fixed values
+  NA_CK(cudaMemcpyAsync(spare0, U2, state_bytes, cudaMemcpyDeviceToDevice, st));
+  NA_CK(cudaMemcpyAsync(spare1, U2, state_bytes, cudaMemcpyDeviceToDevice, st));
+
+  void *buf[4] = {U1, U2, spare0, spare1};
+  int iu1 = 0, iu2 = 1;
+  const int steps = 2 * ((nt + 1) / 2);
+  int left = steps;
+  while (left > 0) {
+    const int T = left < cfg.depth ? left : cfg.depth;
+    int spare[2], n = 0;
+    for (int b = 0; b < 4 && n < 2; b++)
+      if (b != iu1 && b != iu2) spare[n++] = b;
+    FusedLaunch L{};
+    L.prev = buf[iu1];
+    L.cur = buf[iu2];
+    L.out_prev = buf[spare[0]];
+    L.out_cur = buf[spare[1]];
+    L.roc2 = U3;
+    L.steps = T;
+    L.write_prev = (to == 2 || left == T) ? 1 : 0;
+    for (int m = 0; m < 5; m++) L.cc[m] = m <= r ? coefs[m] : 0.0;
+    NA_CK(launch_fused(g, tsz, d->precision, cfg, L, st));
+    iu1 = spare[0];
+    iu2 = spare[1];
+    left -= T;
+  }
+  // move the final states (U1 = state steps-1, U2 = state steps) back into the caller's arrays
+  if (iu2 == 0) {  // current state sits in U1's array: park it in a spare first
+    const int park = iu1 == 2 ? 3 : 2;
+    NA_CK(cudaMemcpyAsync(buf[park], buf[iu2], state_bytes, cudaMemcpyDeviceToDevice, st));
+    iu2 = park;
+  }
+  if (iu1 != 0) NA_CK(cudaMemcpyAsync(buf[0], buf[iu1], state_bytes, cudaMemcpyDeviceToDevice, st));
+  if (iu2 != 1) NA_CK(cudaMemcpyAsync(buf[1], buf[iu2], state_bytes, cudaMemcpyDeviceToDevice, st));
+  NA_CK(cudaStreamSynchronize(st));
+  NA_CK(cudaGetLastError());
+  return 0;
+}

@@ -72,6 +72,8 @@ def lib():
         L.girih_gpu_fill_seeded.argtypes = [P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double),
                                             ctypes.POINTER(ctypes.c_double), ctypes.c_int]
         L.girih_gpu_download_roc2.argtypes = [P, P]
+        L.girih_gpu_fused_run_noalloc.argtypes = [ctypes.POINTER(Desc), P, P, P, ctypes.POINTER(ctypes.c_double),
+                                                  ctypes.c_int, P]
         L.girih_gpu_info.argtypes = [P, ctypes.POINTER(Info)]
         L.girih_gpu_strerror.argtypes = [ctypes.c_int]
         L.girih_gpu_strerror.restype = ctypes.c_char_p
@@ -192,6 +194,25 @@ class Context:
         inf = Info()
         _check(lib().girih_gpu_info(self._h, ctypes.byref(inf)), "girih_gpu_info")
         return {k: (getattr(inf, k).decode() if k == "kernel_name" else getattr(inf, k)) for k, _ in Info._fields_}
+
+
+def fused_run_noalloc(op, nx, ny, nz, U1, U2, U3, coefs, nt, precision="fp64", pnx=None, fusion_depth=0,
+                      device=0, stream=None):
+    """Fused time loop on caller-owned DEVICE arrays (reference layout, raw
+    device addresses) without any device allocation by the library."""
+    r = OP_INFO[op][0]
+    d = Desc()
+    d.target_kernel = op
+    d.stencil_shape[:] = [nx, ny, nz]
+    d.ldomain_shape[:] = [padded_nx(nx, r) if pnx is None else pnx, ny + 2 * r, nz + 2 * r]
+    d.host_real_size = 8 if precision == "fp64" else 4
+    d.precision = PRECISIONS[precision]
+    d.schedule = FUSED
+    d.fusion_depth = fusion_depth
+    d.device = device
+    cc = (ctypes.c_double * 5)(*(list(coefs)[:5] + [0.0] * (5 - len(list(coefs)[:5]))))
+    _check(lib().girih_gpu_fused_run_noalloc(ctypes.byref(d), U1, U2, U3, cc, nt, stream),
+           "girih_gpu_fused_run_noalloc")
 
 
 def rel_errors(norms):

@@ -142,6 +142,28 @@ int girih_gpu_download_roc2(girih_gpu_ctx *c, void *U3);
 
 int girih_gpu_info(girih_gpu_ctx *c, girih_gpu_info_t *info);
 
+/* Time-fused stepping without any device allocation.  This entry point has no
+ * counterpart in the reference.  It is for callers that cannot call cudaMalloc:
+ * a host application that owns the device's memory through its own pool (an
+ * allocation behind its back escapes its accounting or fails under its cap), or
+ * a code path that must not take the device synchronisation cudaMalloc/cudaFree
+ * can cause.  The caller passes its own device arrays U1, U2 (in/out) and U3
+ * (roc2, time-order-2 operators) in the reference layout (ldomain_shape,
+ * element type FP64 for GIRIH_FP64, FP32 otherwise) and the r+1 constant
+ * coefficients; operators 0, 1 and 8; U1 and U2 must carry equal halos.  The
+ * call advances nt steps like girih_gpu_run() (U1 = state steps-1, U2 = state
+ * steps) and returns when the work on `stream` (a cudaStream_t, NULL = default
+ * stream) is done.  The two spare state arrays of the fused schedule live in a
+ * static device array of GIRIH_NOALLOC_SCRATCH_BYTES that every GPU loading
+ * this library holds until the process exits: grids whose two state arrays do
+ * not fit are rejected with GIRIH_GPU_EINVAL.  All calls share that array, so
+ * calls that overlap on the GPU race; serialise them.  The first call on a
+ * device looks up the array's device address, so make it before any stream
+ * capture. */
+#define GIRIH_NOALLOC_SCRATCH_BYTES (64u << 20)
+int girih_gpu_fused_run_noalloc(const girih_gpu_desc *d, void *U1, void *U2, const void *U3,
+                                const double *coefs, int nt, void *stream);
+
 const char *girih_gpu_strerror(int err);
 const char *girih_gpu_last_error(void); /* detail of the calling thread's last error */
 int girih_gpu_abi_version(void);

@@ -19,6 +19,7 @@
 // level below.
 #pragma once
 #include <algorithm>
+#include <utility>
 
 #include "fused.cuh"
 #include "ops.cuh"
@@ -34,22 +35,38 @@ template <class T> struct FusedArgs {
   int write_prev;
 };
 
-template <int R, class T, int QL> struct FusedAcc {
+// z-queue slot of plane p: planes are stored at p mod QL, so advancing a step
+// renames registers instead of moving them (the step loop is unrolled QL times
+// and every slot index below is a compile-time constant).
+template <int QL> __host__ __device__ constexpr int qslot(int x) { return ((x % QL) + QL) % QL; }
+
+template <int R, class T, int QL, int BASE> struct FusedAcc {
   const T *__restrict__ s;  // shared-memory element of the centre (level l-1, plane p)
-  const T (&q)[QL];         // z queue of level l-1
-  static constexpr int CI = QL - 1 - R;
-  static constexpr int LD = 0;  // unused
-  int ld;                    // shared-memory row length
-  __device__ __forceinline__ T c() const { return q[CI]; }
+  const T (&q)[QL];         // z queue of level l-1; plane p sits in slot BASE
+  int ld;                   // shared-memory row length
+  __device__ __forceinline__ T c() const { return q[qslot<QL>(BASE)]; }
   __device__ __forceinline__ T x(int d) const { return s[d]; }
   __device__ __forceinline__ T y(int d) const { return s[d * ld]; }
-  __device__ __forceinline__ T z(int d) const { return q[CI + d]; }
+  __device__ __forceinline__ T z(int d) const { return q[qslot<QL>(BASE + d)]; }
 };
 
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-  s = __fadd_rn(a, b);
-  float bb = __fsub_rn(s, a);
-  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+template <class F, int... I>
+__device__ __forceinline__ void static_for_impl(F &f, std::integer_sequence<int, I...>) {
+  (f(std::integral_constant<int, I>{}), ...);
+}
+template <int N, class F> __device__ __forceinline__ void static_for(F &&f) {
+  static_for_impl(f, std::make_integer_sequence<int, N>{});
+}
+
+// Compensated leapfrog update 2v - u + roc2*lap: the cancellation 2v - u is
+// computed exactly as s + e (two-sum), e is folded into the small term, and the
+// result is rounded once.
+__device__ __forceinline__ float leapfrog_compensated(float v, float u, float r2, float lap) {
+  const float a = 2.f * v;
+  const float s = __fsub_rn(a, u);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(-u, bb));
+  return __fadd_rn(s, fmaf(r2, lap, e));
 }
 
 template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY>
@@ -58,12 +75,12 @@ __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
   constexpr int TO = OpTraits<OP>::TO;
   constexpr int D = R + 1;
   constexpr int QL = TO == 2 ? 2 * R + 2 : 2 * R + 1;
-  constexpr int CI = QL - 1 - R;
   constexpr int RY = NTY * CY;
   constexpr int H = TT * R;
   constexpr int BX = NTX - 2 * H;
   constexpr int BY = RY - 2 * H;
   static_assert(BX > 0 && BY > 0, "tile too small for the fusion depth");
+  static_assert(TT * CY <= 32, "activity mask holds 32 (level, row) pairs");
 
   extern __shared__ __align__(16) unsigned char smraw[];
   T *sm = reinterpret_cast<T *>(smraw);  // [2][TT][RY][NTX]
@@ -76,6 +93,7 @@ __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
   const int Z1 = min(Z0 + a.zchunk, g.nnz - R);
   const int sb = max(0, Z0 - H);
   const int se = Z1 - 1 + TT * D;
+  const int s0 = sb - sb % QL;  // aligned so that plane p lives in slot p mod QL
 
   const int xi = X0 - H + tx;  // interior x index of this column
   const int i = xi + R;        // reference x index
@@ -83,17 +101,22 @@ __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
   const bool x_int = xi >= 0 && xi < g.nx;
   const bool x_out = tx >= H && tx < NTX - H && xi < g.nx;
 
-  bool y_dom[CY], y_int[CY], y_out[CY];
+  bool y_dom[CY], y_out[CY];
   int64_t col[CY];
+  unsigned act_mask = 0;  // bit (l-1)*CY + c: level l of row c lies in the shrinking valid region
 #pragma unroll
   for (int c = 0; c < CY; c++) {
     const int ry = ty + c * NTY;
     const int yj = Y0 - H + ry;
     const int j = yj + R;
     y_dom[c] = j >= 0 && j < g.nny;
-    y_int[c] = yj >= 0 && yj < g.ny;
-    y_out[c] = ry >= H && ry < RY - H && yj < g.ny;
+    const bool y_int = yj >= 0 && yj < g.ny;
+    y_out[c] = x_out && ry >= H && ry < RY - H && yj < g.ny;
     col[c] = (x_dom && y_dom[c]) ? (int64_t)j * g.px + g.ox + i : 0;
+#pragma unroll
+    for (int l = 1; l <= TT; l++)
+      if (x_int && y_int && tx >= l * R && tx < NTX - l * R && ry >= l * R && ry < RY - l * R)
+        act_mask |= 1u << ((l - 1) * CY + c);
   }
 
   T cc[5];
@@ -101,103 +124,83 @@ __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
   for (int m = 0; m < 5; m++) cc[m] = a.cc[m];
 
   T q[TT][CY][QL];
-  float ql[COMP ? TT : 1][CY][COMP ? QL : 1];
 #pragma unroll
   for (int l = 0; l < TT; l++)
 #pragma unroll
     for (int c = 0; c < CY; c++)
 #pragma unroll
-      for (int e = 0; e < QL; e++) {
-        q[l][c][e] = T(0);
-        if constexpr (COMP) ql[l][c][e] = 0.f;
-      }
+      for (int e = 0; e < QL; e++) q[l][c][e] = T(0);
 
-  for (int s = sb; s <= se; ++s) {
-    const int rb = (s - 1) & 1, wb = s & 1;
-    // levels TT..1, highest first: level l reads level l-1's queue before
-    // level l-1 pushes this step's plane
+  for (int sbase = s0; sbase <= se; sbase += QL) {
+    static_for<QL>([&](auto ph_c) {
+      constexpr int PH = decltype(ph_c)::value;
+      const int s = sbase + PH;
+      if (s > se) return;  // uniform over the CTA
+      const int rb = (s - 1) & 1, wb = s & 1;
+      const int64_t soff = (int64_t)s * plane;
+      // levels TT..1, highest first: level l reads level l-1's queue before
+      // level l-1 stores this step's plane
+      static_for<TT>([&](auto li_c) {
+        constexpr int L = TT - decltype(li_c)::value;  // TT, TT-1, ..., 1
+        constexpr int SL = qslot<QL>(PH - L * D);        // slot of plane p in every queue
+        const int p = s - L * D;
+        const bool p_int = p >= R && p < g.nnz - R;
+        const bool p_out = p_int && p >= Z0 && p < Z1;
+        const int64_t poff = soff - (int64_t)(L * D) * plane;
+        const T *smr = sm + (size_t)((rb * TT + (L - 1)) * RY) * NTX;
 #pragma unroll
-    for (int l = TT; l >= 1; --l) {
-      const int p = s - l * D;
-      const bool p_int = p >= R && p < g.nnz - R;
-      const bool p_out = p >= Z0 && p < Z1;
-      const T *smr = sm + (size_t)((rb * TT + (l - 1)) * RY) * NTX;
-#pragma unroll
-      for (int c = 0; c < CY; c++) {
-        const int ry = ty + c * NTY;
-        const bool act = tx >= l * R && tx < NTX - l * R && ry >= l * R && ry < RY - l * R &&
-                         x_int && y_int[c] && p_int;
-        T val = q[l - 1][c][CI];
-        float vlo = 0.f;
-        if constexpr (COMP) vlo = ql[l - 1][c][CI];
-        if (act) {
-          const int64_t at = (int64_t)p * plane + col[c];
-          FusedAcc<R, T, QL> acc{smr + ry * NTX + tx, q[l - 1][c], NTX};
-          if constexpr (TO == 2) {
-            T uold = l >= 2 ? q[l - 2 < 0 ? 0 : l - 2][c][0] : a.prev[at];
-            T r2 = __ldg(a.roc2 + at);
-            if constexpr (COMP) {
-              // compensated leapfrog: (hi, lo) state within the pass,
-              // 2v - u + roc2*lap with an error-free two-sum
-              const float ulo = l >= 2 ? ql[l - 2 < 0 ? 0 : l - 2][c][0] : 0.f;
-              const float lap = star_const_sum<R, FastArith>(cc, acc);
-              float s1, e1;
-              two_sum(2.f * val, -uold, s1, e1);
-              const float lo = fmaf(r2, lap, e1 + (2.f * vlo - ulo));
-              float hi, lo2;
-              two_sum(s1, lo, hi, lo2);
-              val = hi;
-              vlo = lo2;
+        for (int c = 0; c < CY; c++) {
+          const int ry = ty + c * NTY;
+          T val = q[L - 1][c][SL];
+          if (p_int && (act_mask >> ((L - 1) * CY + c) & 1u)) {
+            const int64_t at = poff + col[c];
+            FusedAcc<R, T, QL, SL> acc{smr + ry * NTX + tx, q[L - 1][c], NTX};
+            if constexpr (TO == 2) {
+              T uold;
+              if constexpr (L >= 2) uold = q[L - 2][c][SL];
+              else uold = a.prev[at];
+              const T r2 = __ldg(a.roc2 + at);
+              if constexpr (COMP) {
+                const float lap = star_const_sum<R, FastArith>(cc, acc);
+                val = leapfrog_compensated(val, uold, r2, lap);
+              } else {
+                CoefFull<T> none{nullptr, 0};
+                val = apply_op<OP, FastArith>(cc, none, 0, acc, uold, r2);
+              }
             } else {
               CoefFull<T> none{nullptr, 0};
-              val = apply_op<OP, FastArith>(cc, none, 0, acc, uold, r2);
+              val = apply_op<OP, FastArith>(cc, none, 0, acc, T(0), T(0));
             }
-          } else {
-            CoefFull<T> none{nullptr, 0};
-            val = apply_op<OP, FastArith>(cc, none, 0, acc, T(0), T(0));
           }
-        }
-        if (p_int && p_out && x_out && y_out[c]) {
-          const int64_t at = (int64_t)p * plane + col[c];
-          if (l == TT) a.out_cur[at] = val;
-          if (l == TT - 1 && a.write_prev) a.out_prev[at] = val;
-        }
-        if (l < TT) {
-#pragma unroll
-          for (int e = 0; e < QL - 1; e++) q[l][c][e] = q[l][c][e + 1];
-          q[l][c][QL - 1] = val;
-          if constexpr (COMP) {
-#pragma unroll
-            for (int e = 0; e < QL - 1; e++) ql[l][c][e] = ql[l][c][e + 1];
-            ql[l][c][QL - 1] = vlo;
+          if (p_out && y_out[c]) {
+            if constexpr (L == TT) a.out_cur[poff + col[c]] = val;
+            if constexpr (L == TT - 1) {
+              if (a.write_prev) a.out_prev[poff + col[c]] = val;
+            }
           }
+          if constexpr (L < TT) q[L][c][SL] = val;
+        }
+      });
+      // level 0: stream plane s from HBM
+      const bool s_in = s < g.nnz;
+#pragma unroll
+      for (int c = 0; c < CY; c++) {
+        T v = T(0);
+        if (s_in && x_dom && y_dom[c]) v = __ldg(a.cur + soff + col[c]);
+        q[0][c][qslot<QL>(PH)] = v;
+        if constexpr (TT == 1) {
+          if (a.write_prev && s >= R && s < g.nnz - R && s >= Z0 && s < Z1 && y_out[c])
+            a.out_prev[soff + col[c]] = v;
         }
       }
-    }
-    // level 0: stream plane s from HBM
-    const bool s_in = s < g.nnz;
+      // publish each level's centre plane (s - l*D - R) for the x/y neighbours of step s+1
 #pragma unroll
-    for (int c = 0; c < CY; c++) {
-      T v = T(0);
-      if (s_in && x_dom && y_dom[c]) v = __ldg(a.cur + (int64_t)s * plane + col[c]);
+      for (int l = 0; l < TT; l++)
 #pragma unroll
-      for (int e = 0; e < QL - 1; e++) q[0][c][e] = q[0][c][e + 1];
-      q[0][c][QL - 1] = v;
-      if constexpr (COMP) {
-#pragma unroll
-        for (int e = 0; e < QL - 1; e++) ql[0][c][e] = ql[0][c][e + 1];
-        ql[0][c][QL - 1] = 0.f;
-      }
-      if (TT == 1 && a.write_prev && s >= R && s < g.nnz - R && s >= Z0 && s < Z1 && x_out && y_out[c])
-        a.out_prev[(int64_t)s * plane + col[c]] = v;
-    }
-    // publish each level's centre plane for the x/y neighbours of step s+1
-#pragma unroll
-    for (int l = 0; l < TT; l++)
-#pragma unroll
-      for (int c = 0; c < CY; c++)
-        sm[(size_t)((wb * TT + l) * RY + ty + c * NTY) * NTX + tx] = q[l][c][CI];
-    __syncthreads();
+        for (int c = 0; c < CY; c++)
+          sm[(size_t)((wb * TT + l) * RY + ty + c * NTY) * NTX + tx] = q[l][c][qslot<QL>(PH - l * D - R)];
+      __syncthreads();
+    });
   }
 }
 

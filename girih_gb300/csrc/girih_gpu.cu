@@ -6,9 +6,14 @@
 // between two CUDA events on that stream, which replaces the reference's
 // MPI_Wtime bracket around the stepper (src/performance.c:74-78).
 #include <algorithm>
+#include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
 #include <string>
+#include <tuple>
+#include <vector>
 
 #include "internal.cuh"
 #include "fused.cuh"
@@ -84,6 +89,26 @@ struct girih_gpu_ctx {
 };
 
 namespace {
+
+// Autotuner choices, per (operator, precision, size class).
+struct TuneChoice {
+  int sched, variant, depth;
+};
+std::mutex g_tune_mutex;
+std::map<std::tuple<int, int, int>, TuneChoice> g_tune_cache;
+
+int size_class(const Geom &g) {
+  double pts = (double)g.nx * g.ny * g.nz;
+  return (int)std::floor(std::log2(pts > 1 ? pts : 1));
+}
+
+bool cached_choice(const Geom &g, int precision, TuneChoice *out) {
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  auto it = g_tune_cache.find(std::make_tuple(g.op, precision, size_class(g)));
+  if (it == g_tune_cache.end()) return false;
+  *out = it->second;
+  return true;
+}
 
 struct DeviceGuard {
   int prev = -1;
@@ -359,7 +384,13 @@ int girih_gpu_create(girih_gpu_ctx **out, const girih_gpu_desc *d) {
     sched = ok && !d->exact ? GIRIH_SCHED_FUSED : GIRIH_SCHED_PLAIN;
   }
   c->sched = sched;
-  if (sched == GIRIH_SCHED_FUSED) {
+  TuneChoice tc{};
+  const bool untuned = d->fusion_depth == 0 && d->block_x == 0 && d->block_y == 0;
+  if (sched != GIRIH_SCHED_PLAIN && untuned && cached_choice(c->g, d->precision, &tc)) {
+    if (d->schedule == GIRIH_SCHED_AUTO) c->sched = sched = tc.sched;
+    if (tc.sched == GIRIH_SCHED_FUSED) c->fcfg = make_fused_config(c->g, d->precision, tc.depth, tc.variant);
+  }
+  if (sched == GIRIH_SCHED_FUSED && !c->fcfg.depth) {
     c->fcfg = choose_fused_config(c->g, d->precision, d->fusion_depth, d->block_x, d->block_y);
     if (!c->fcfg.depth) {
       delete c;
@@ -442,6 +473,8 @@ int girih_gpu_upload(girih_gpu_ctx *c, const void *U1, const void *U2, const voi
   c->iu1 = 0;
   c->iu2 = 1;
   if ((e = check_halos(c))) return e;
+  if (c->sched == GIRIH_SCHED_FUSED && !c->halos_equal && c->d.schedule == GIRIH_SCHED_AUTO)
+    c->sched = GIRIH_SCHED_PLAIN;  // unequal halos: keep the exact ping-pong of the plain schedule
   if (c->sched == GIRIH_SCHED_FUSED && !c->halos_equal)
     return fail(GIRIH_GPU_EUNSUPPORTED,
                 "fused schedule needs identical U1/U2 halos (the reference initialises them equal)");
@@ -618,6 +651,98 @@ int girih_gpu_compare(girih_gpu_ctx *a, girih_gpu_ctx *b, double out[4]) {
   else
     CK(launch_norms<float, float>(a->g, (const float *)pa, nullptr, b->g, (const float *)pb, a->acc, a->st));
   return read_norms(a, out);
+}
+
+int girih_gpu_autotune(girih_gpu_ctx *c, int trial_steps, girih_gpu_info_t *chosen) {
+  if (!c) return fail(GIRIH_GPU_EINVAL, "null context");
+  if (!c->uploaded) return fail(GIRIH_GPU_ESTATE, "autotune before upload");
+  DeviceGuard dg(c->d.device);
+  const Geom &g = c->g;
+  const int prec = c->d.precision;
+  std::vector<TuneChoice> cands;
+  const bool explicit_cfg = c->d.fusion_depth != 0 || c->d.block_x != 0 || c->d.block_y != 0;
+  if (c->d.schedule == GIRIH_SCHED_AUTO || (c->d.schedule == GIRIH_SCHED_PLAIN))
+    cands.push_back({GIRIH_SCHED_PLAIN, 0, 1});
+  if (c->d.schedule != GIRIH_SCHED_PLAIN && !c->d.exact && fused_supported(g, prec) && c->halos_equal) {
+    for (int v = 0; v < FV_COUNT; v++)
+      for (int t = 1; t <= fused_max_depth(g, prec); t++) {
+        FusedConfig fc = make_fused_config(g, prec, t, v);
+        if (!fc.depth) continue;
+        if (explicit_cfg && ((c->d.fusion_depth && t != c->d.fusion_depth) || (c->d.block_x && fc.bx != c->d.block_x) ||
+                             (c->d.block_y && fc.by != c->d.block_y)))
+          continue;
+        cands.push_back({GIRIH_SCHED_FUSED, v, t});
+      }
+  }
+  if (cands.empty()) return girih_gpu_info(c, chosen);
+  int e = 0;
+  if (cands.size() > 1 || cands[0].sched == GIRIH_SCHED_FUSED) {
+    if (!c->f[2] && (e = ensure_fused_buffers(c))) return e;
+    for (int b = 2; b < 4; b++)  // spare buffers carry the fixed halo
+      CK(cudaMemcpyAsync(c->f[b], c->f[c->iu2], (size_t)g.elems * c->tsz, cudaMemcpyDeviceToDevice, c->st));
+  }
+  // back up the state so that tuning leaves the grid unchanged
+  void *bk[2] = {nullptr, nullptr};
+  const size_t fb = (size_t)g.elems * c->tsz;
+  auto free_bk = [&]() {
+    for (void *p : bk)
+      if (p) {
+        cudaFree(p);
+        c->dev_bytes -= (double)fb;
+      }
+  };
+  if ((e = dev_alloc(c, &bk[0], fb)) || (e = dev_alloc(c, &bk[1], fb))) {
+    free_bk();
+    return e;
+  }
+  CK(cudaMemcpyAsync(bk[0], c->f[c->iu1], fb, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaMemcpyAsync(bk[1], c->f[c->iu2], fb, cudaMemcpyDeviceToDevice, c->st));
+  const int steps = trial_steps > 0 ? 2 * ((trial_steps + 1) / 2) : (g.r == 4 ? 8 : 24);
+  const int saved_sched = c->sched;
+  const FusedConfig saved_cfg = c->fcfg;
+  double best = 1e300;
+  TuneChoice best_c = cands[0];
+  drop_graph(c);
+  for (const TuneChoice &tc : cands) {
+    c->sched = tc.sched;
+    c->fcfg = tc.sched == GIRIH_SCHED_FUSED ? make_fused_config(g, prec, tc.depth, tc.variant) : FusedConfig{};
+    float ms_min = 1e30f;
+    for (int rep = 0; rep < 3; rep++) {
+      int a = c->iu1, b = c->iu2, launches = 0;
+      CK(cudaEventRecord(c->e0, c->st));
+      if ((e = issue_steps(c, steps, &launches, &a, &b))) {
+        free_bk();
+        return e;
+      }
+      CK(cudaEventRecord(c->e1, c->st));
+      CK(cudaEventSynchronize(c->e1));
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, c->e0, c->e1));
+      if (rep > 0) ms_min = std::min(ms_min, ms);  // first repetition warms up
+      c->iu1 = a;
+      c->iu2 = b;
+    }
+    if (ms_min < best) {
+      best = ms_min;
+      best_c = tc;
+    }
+  }
+  // restore the state into the first two buffers
+  CK(cudaMemcpyAsync(c->f[0], bk[0], fb, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaMemcpyAsync(c->f[1], bk[1], fb, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  free_bk();
+  c->iu1 = 0;
+  c->iu2 = 1;
+  (void)saved_sched;
+  (void)saved_cfg;
+  c->sched = best_c.sched;
+  c->fcfg = best_c.sched == GIRIH_SCHED_FUSED ? make_fused_config(g, prec, best_c.depth, best_c.variant) : FusedConfig{};
+  if (!explicit_cfg) {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tune_cache[std::make_tuple(g.op, prec, size_class(g))] = best_c;
+  }
+  return girih_gpu_info(c, chosen);
 }
 
 int girih_gpu_info(girih_gpu_ctx *c, girih_gpu_info_t *info) {

@@ -75,6 +75,7 @@ def lib():
         L.girih_gpu_fused_run_noalloc.argtypes = [ctypes.POINTER(Desc), P, P, P, ctypes.POINTER(ctypes.c_double),
                                                   ctypes.c_int, P]
         L.girih_gpu_info.argtypes = [P, ctypes.POINTER(Info)]
+        L.girih_gpu_autotune.argtypes = [P, ctypes.c_int, ctypes.POINTER(Info)]
         L.girih_gpu_strerror.argtypes = [ctypes.c_int]
         L.girih_gpu_strerror.restype = ctypes.c_char_p
         L.girih_gpu_last_error.restype = ctypes.c_char_p
@@ -189,6 +190,12 @@ class Context:
         out = (ctypes.c_double * 4)()
         _check(lib().girih_gpu_compare(self._h, ref_ctx._h, out), "girih_gpu_compare")
         return list(out)
+
+    def autotune(self, trial_steps=0):
+        """Time the candidate schedules/tiles/depths on this grid and keep the fastest."""
+        inf = Info()
+        _check(lib().girih_gpu_autotune(self._h, trial_steps, ctypes.byref(inf)), "girih_gpu_autotune")
+        return {k: (getattr(inf, k).decode() if k == "kernel_name" else getattr(inf, k)) for k, _ in Info._fields_}
 
     def info(self):
         inf = Info()

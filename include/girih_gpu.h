@@ -142,6 +142,16 @@ int girih_gpu_download_roc2(girih_gpu_ctx *c, void *U3);
 
 int girih_gpu_info(girih_gpu_ctx *c, girih_gpu_info_t *info);
 
+/* Autotuner (replaces the reference's CPU tile auto-tuning, auto_tune_params in
+ * src/kernels/diamond_utils.c:691-847): times, on this context's own grid, each
+ * candidate the schedule allows -- the plain kernel (GIRIH_SCHED_AUTO only) and
+ * every fused tile shape and fusion depth -- over trial_steps steps (0 = a
+ * default), keeps the fastest and restores the grid state.  Choices are cached
+ * per operator, precision and size class (log2 of the point count), and later
+ * contexts created with fusion_depth = 0 and no tile pick them up.  *chosen
+ * (may be NULL) receives the result. */
+int girih_gpu_autotune(girih_gpu_ctx *c, int trial_steps, girih_gpu_info_t *chosen);
+
 /* Time-fused stepping without any device allocation.  This entry point has no
  * counterpart in the reference.  It is for callers that cannot call cudaMalloc:
  * a host application that owns the device's memory through its own pool (an

@@ -121,3 +121,23 @@ def test_auto_schedule_picks_fused_where_provided():
     for op, want in ((1, gpu.FUSED), (8, gpu.FUSED), (0, gpu.FUSED), (5, gpu.PLAIN)):
         with gpu.Context(op, 32, 32, 32, schedule="auto") as ctx:
             assert ctx.info()["schedule"] == want
+
+
+@pytest.mark.parametrize("op,precision,sched", [(8, "mixed", "fused"), (1, "fp64", "auto"), (0, "fp32", "fused")])
+def test_autotune_restores_state_and_stays_correct(op, precision, sched):
+    g0 = oracle_grid(op, *_shape(op), seed=4)
+    nt = 10
+    ref = g0.copy().run(nt, nthreads=4)
+    with gpu_context(g0.copy(), precision=precision, schedule=sched) as ctx:
+        chosen = ctx.autotune(trial_steps=6)
+        u1, u2 = ctx.download()
+        np.testing.assert_array_equal(u1, g0.U1.astype(np.float32).astype(np.float64) if precision != "fp64" else g0.U1)
+        assert chosen["schedule"] in (gpu.PLAIN, gpu.FUSED)
+        ctx.run(nt)
+        u1, _ = ctx.download()
+    tol = FP64_TOL if precision == "fp64" else 5e-6
+    assert max_rel(u1, ref.U1, ref) <= tol
+    # a later context of the same operator, precision and size class reuses the choice
+    with gpu.Context(op, *_shape(op), precision=precision, schedule=sched) as ctx2:
+        i2 = ctx2.info()
+        assert (i2["schedule"], i2["fusion_depth"]) == (chosen["schedule"], chosen["fusion_depth"])

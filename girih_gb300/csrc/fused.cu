@@ -11,14 +11,18 @@ bool fused_supported(const Geom &g, int precision) {
 
 int fused_max_depth(const Geom &g, int precision) {
   if (g.r == 4) return 2;
-  return precision == GIRIH_FP64 ? 4 : 6;
+  return precision == GIRIH_FP64 ? 2 : 4;
 }
 
-// Column region of one CTA: variant 0 = 64 x 32 (64x16 threads, 2 rows each),
-// variant 1 = 32 x 64 (32x16 threads, 4 rows each).
-static void variant_shape(int v, int *ntx, int *ry) {
+// Column region of one CTA (every thread owns an x pair):
+//   radius 1 (x pairs per thread): variant 0 = 64 x 32 (32x16 threads, 2 rows
+//   each), variant 1 = 32 x 64 (16x64 threads, 1 row each);
+//   radius 4 (one column per thread): variant 0 = 64 x 32 (64x16 threads, 2
+//   rows), variant 1 = 32 x 64 (32x32 threads, 2 rows).
+static void variant_shape(int v, int r, int *ntx, int *ry, int *vx) {
   *ntx = v == 0 ? 64 : 32;
   *ry = v == 0 ? 32 : 64;
+  *vx = r == 1 ? 2 : 1;
 }
 
 FusedConfig make_fused_config(const Geom &g, int precision, int depth, int variant) {
@@ -26,11 +30,14 @@ FusedConfig make_fused_config(const Geom &g, int precision, int depth, int varia
   if (!fused_supported(g, precision) || depth < 1 || depth > fused_max_depth(g, precision) ||
       variant < 0 || variant >= FV_COUNT)
     return c;
-  int ntx, ry;
-  variant_shape(variant, &ntx, &ry);
+  int ntx, ry, vx;
+  variant_shape(variant, g.r, &ntx, &ry, &vx);
+  // double-buffered shared memory of all levels must fit one CTA (227 KiB)
+  const size_t tsz = precision == GIRIH_FP64 ? 8 : 4;
+  if ((size_t)2 * depth * ntx * ry * tsz > (size_t)227 * 1024) return c;
   c.depth = depth;
   c.variant = variant;
-  c.bx = ntx - 2 * depth * g.r;
+  c.bx = ntx - 2 * depth * g.r - (vx - 1);  // pairs lose one column to their alignment
   c.by = ry - 2 * depth * g.r;
   if (c.bx <= 0 || c.by <= 0) c.depth = 0;
   return c;

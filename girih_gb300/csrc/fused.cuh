@@ -7,7 +7,7 @@ namespace girih {
 // Thread-block shapes of the fused kernel.  A CTA covers an input region of
 // NTX x (NTY*CY) columns (tile + halo of depth*R on every side); each thread
 // owns one x column and CY rows of it and streams the whole z range.
-enum FusedVariant { FV_64x16x2 = 0, FV_32x16x4 = 1, FV_COUNT = 2 };
+enum FusedVariant { FV_64x32_512 = 0, FV_32x64_1024 = 1, FV_COUNT = 2 };
 
 struct FusedConfig {
   int depth = 0;    // time steps per pass (0 = not available)

@@ -40,14 +40,47 @@ template <class T> struct FusedArgs {
 // and every slot index below is a compile-time constant).
 template <int QL> __host__ __device__ constexpr int qslot(int x) { return ((x % QL) + QL) % QL; }
 
-template <int R, class T, int QL, int BASE> struct FusedAcc {
-  const T *__restrict__ s;  // shared-memory element of the centre (level l-1, plane p)
-  const T (&q)[QL];         // z queue of level l-1; plane p sits in slot BASE
-  int ld;                   // shared-memory row length
-  __device__ __forceinline__ T c() const { return q[qslot<QL>(BASE)]; }
-  __device__ __forceinline__ T x(int d) const { return s[d]; }
-  __device__ __forceinline__ T y(int d) const { return s[d * ld]; }
-  __device__ __forceinline__ T z(int d) const { return q[qslot<QL>(BASE + d)]; }
+// Vector of VX consecutive x elements (one thread owns VX columns).
+template <class T, int VX> struct VecT;
+template <> struct VecT<float, 1> { using type = float; };
+template <> struct VecT<float, 2> { using type = float2; };
+template <> struct VecT<double, 1> { using type = double; };
+template <> struct VecT<double, 2> { using type = double2; };
+
+template <class T, int VX> struct Pack {
+  T e[VX];
+  __device__ __forceinline__ void load(const T *p) {
+    using V = typename VecT<T, VX>::type;
+    if constexpr (VX == 1) e[0] = p[0];
+    else { V v = *reinterpret_cast<const V *>(p); e[0] = v.x; e[1] = v.y; }
+  }
+  __device__ __forceinline__ void ldg(const T *p) {
+    using V = typename VecT<T, VX>::type;
+    if constexpr (VX == 1) e[0] = __ldg(p);
+    else { V v = __ldg(reinterpret_cast<const V *>(p)); e[0] = v.x; e[1] = v.y; }
+  }
+  __device__ __forceinline__ void store(T *p) const {
+    using V = typename VecT<T, VX>::type;
+    if constexpr (VX == 1) p[0] = e[0];
+    else { V v; v.x = e[0]; v.y = e[1]; *reinterpret_cast<V *>(p) = v; }
+  }
+};
+
+// Neighbour accessor of element V of a thread's x-group at level l-1, plane p
+// (slot BASE of the z queues): x neighbours inside the group come from
+// registers, the others from the shared-memory row; y neighbours from the
+// pre-loaded shared-memory vectors; z neighbours from the z queue.
+template <int R, class T, int QL, int BASE, int VX, int V> struct FusedAcc {
+  const T *__restrict__ srow;             // shared-memory row of level l-1 at this thread's first column
+  const T (&q)[VX][QL];                   // z queues of the thread's columns (level l-1)
+  const T (&yv)[2 * R][VX];               // y neighbours: [d-1] = +d, [R+d-1] = -d
+  __device__ __forceinline__ T c() const { return q[V][qslot<QL>(BASE)]; }
+  __device__ __forceinline__ T x(int d) const {
+    const int pos = V + d;
+    return (pos >= 0 && pos < VX) ? q[pos < 0 ? 0 : (pos >= VX ? VX - 1 : pos)][qslot<QL>(BASE)] : srow[pos];
+  }
+  __device__ __forceinline__ T y(int d) const { return d > 0 ? yv[d - 1][V] : yv[R - d - 1][V]; }
+  __device__ __forceinline__ T z(int d) const { return q[V][qslot<QL>(BASE + d)]; }
 };
 
 template <class F, int... I>
@@ -69,21 +102,24 @@ __device__ __forceinline__ float leapfrog_compensated(float v, float u, float r2
   return __fadd_rn(s, fmaf(r2, lap, e));
 }
 
-template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY>
+__device__ __forceinline__ int pmod(int a, int m) { return ((a % m) + m) % m; }
+
+template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX>
 __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
   constexpr int R = OpTraits<OP>::R;
   constexpr int TO = OpTraits<OP>::TO;
   constexpr int D = R + 1;
   constexpr int QL = TO == 2 ? 2 * R + 2 : 2 * R + 1;
-  constexpr int RY = NTY * CY;
+  constexpr int RW = NTX * VX;  // region width (columns)
+  constexpr int RY = NTY * CY;  // region height (rows)
   constexpr int H = TT * R;
-  constexpr int BX = NTX - 2 * H;
+  constexpr int BX = RW - 2 * H - (VX - 1);
   constexpr int BY = RY - 2 * H;
   static_assert(BX > 0 && BY > 0, "tile too small for the fusion depth");
-  static_assert(TT * CY <= 32, "activity mask holds 32 (level, row) pairs");
+  static_assert(TT * CY * VX <= 32, "activity mask holds 32 (level, row, column) bits");
 
   extern __shared__ __align__(16) unsigned char smraw[];
-  T *sm = reinterpret_cast<T *>(smraw);  // [2][TT][RY][NTX]
+  T *sm = reinterpret_cast<T *>(smraw);  // [2][TT][RY][RW]
 
   const Geom &g = a.g;
   const int64_t plane = g.plane;
@@ -95,41 +131,57 @@ __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
   const int se = Z1 - 1 + TT * D;
   const int s0 = sb - sb % QL;  // aligned so that plane p lives in slot p mod QL
 
-  const int xi = X0 - H + tx;  // interior x index of this column
-  const int i = xi + R;        // reference x index
-  const bool x_dom = i >= 0 && i < g.nnx;
-  const bool x_int = xi >= 0 && xi < g.nx;
-  const bool x_out = tx >= H && tx < NTX - H && xi < g.nx;
+  // region start, aligned so that every thread's x-group is one aligned vector in memory
+  const int xs = X0 - H - pmod(X0 - H + R + g.ox, VX);
+  const int xi0 = xs + tx * VX;  // interior x index of the thread's first column
 
-  bool y_dom[CY], y_out[CY];
-  int64_t col[CY];
-  unsigned act_mask = 0;  // bit (l-1)*CY + c: level l of row c lies in the shrinking valid region
+  bool x_dom[VX], x_outc[VX];
+  unsigned x_act = 0;  // bit (l-1)*VX + v: column v inside level l's valid x range
 #pragma unroll
-  for (int c = 0; c < CY; c++) {
-    const int ry = ty + c * NTY;
-    const int yj = Y0 - H + ry;
-    const int j = yj + R;
-    y_dom[c] = j >= 0 && j < g.nny;
-    const bool y_int = yj >= 0 && yj < g.ny;
-    y_out[c] = x_out && ry >= H && ry < RY - H && yj < g.ny;
-    col[c] = (x_dom && y_dom[c]) ? (int64_t)j * g.px + g.ox + i : 0;
+  for (int v = 0; v < VX; v++) {
+    const int xi = xi0 + v;
+    x_dom[v] = xi + R >= 0 && xi + R < g.nnx;
+    const bool x_int = xi >= 0 && xi < g.nx;
+    x_outc[v] = x_int && xi >= X0 && xi < X0 + BX;
 #pragma unroll
     for (int l = 1; l <= TT; l++)
-      if (x_int && y_int && tx >= l * R && tx < NTX - l * R && ry >= l * R && ry < RY - l * R)
-        act_mask |= 1u << ((l - 1) * CY + c);
+      if (x_int && xi >= X0 - (TT - l) * R && xi < X0 + BX + (TT - l) * R) x_act |= 1u << ((l - 1) * VX + v);
   }
+  const bool xg_dom = x_dom[0] && x_dom[VX - 1];
+
+  bool y_dom[CY], y_outr[CY];
+  int64_t col[CY];
+  unsigned act = 0;  // bit ((l-1)*CY + c)*VX + v
+#pragma unroll
+  for (int c = 0; c < CY; c++) {
+    const int yj = Y0 - H + ty + c * NTY;
+    y_dom[c] = yj + R >= 0 && yj + R < g.nny;
+    const bool y_int = yj >= 0 && yj < g.ny;
+    y_outr[c] = y_int && yj >= Y0 && yj < Y0 + BY;
+    col[c] = (int64_t)(yj + R) * g.px + g.ox + (xi0 + R);
+#pragma unroll
+    for (int l = 1; l <= TT; l++)
+      if (y_int && yj >= Y0 - (TT - l) * R && yj < Y0 + BY + (TT - l) * R)
+#pragma unroll
+        for (int v = 0; v < VX; v++)
+          if (x_act >> ((l - 1) * VX + v) & 1u) act |= 1u << (((l - 1) * CY + c) * VX + v);
+  }
+  auto bit = [&](int l, int c, int v) -> bool { return act >> (((l - 1) * CY + c) * VX + v) & 1u; };
+  auto any = [&](int l, int c) -> bool { return (act >> (((l - 1) * CY + c) * VX)) & ((1u << VX) - 1); };
 
   T cc[5];
 #pragma unroll
   for (int m = 0; m < 5; m++) cc[m] = a.cc[m];
 
-  T q[TT][CY][QL];
+  T q[TT][CY][VX][QL];
 #pragma unroll
   for (int l = 0; l < TT; l++)
 #pragma unroll
     for (int c = 0; c < CY; c++)
 #pragma unroll
-      for (int e = 0; e < QL; e++) q[l][c][e] = T(0);
+      for (int v = 0; v < VX; v++)
+#pragma unroll
+        for (int e = 0; e < QL; e++) q[l][c][v][e] = T(0);
 
   for (int sbase = s0; sbase <= se; sbase += QL) {
     static_for<QL>([&](auto ph_c) {
@@ -138,7 +190,24 @@ __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
       if (s > se) return;  // uniform over the CTA
       const int rb = (s - 1) & 1, wb = s & 1;
       const int64_t soff = (int64_t)s * plane;
-      // levels TT..1, highest first: level l reads level l-1's queue before
+      // roc2 (and, for level 1, the old state) of level l are loaded while level
+      // l+1 computes: two levels' worth of registers, latency overlapped
+      Pack<T, VX> r2c[2][CY], pvc[CY];
+      auto issue = [&](int l) {
+        if constexpr (TO == 2) {
+          const int p = s - l * D;
+          const bool p_int = p >= R && p < g.nnz - R;
+#pragma unroll
+          for (int c = 0; c < CY; c++)
+            if (p_int && any(l, c)) {
+              const int64_t at = (int64_t)p * plane + col[c];
+              r2c[l & 1][c].ldg(a.roc2 + at);
+              if (l == 1) pvc[c].ldg(a.prev + at);
+            }
+        }
+      };
+      issue(TT);
+      // levels TT..1, highest first: level l reads level l-1's queues before
       // level l-1 stores this step's plane
       static_for<TT>([&](auto li_c) {
         constexpr int L = TT - decltype(li_c)::value;  // TT, TT-1, ..., 1
@@ -147,73 +216,118 @@ __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
         const bool p_int = p >= R && p < g.nnz - R;
         const bool p_out = p_int && p >= Z0 && p < Z1;
         const int64_t poff = soff - (int64_t)(L * D) * plane;
-        const T *smr = sm + (size_t)((rb * TT + (L - 1)) * RY) * NTX;
+        const T *smr = sm + (size_t)((rb * TT + (L - 1)) * RY) * RW;
+        if constexpr (L > 1) issue(L - 1);
 #pragma unroll
         for (int c = 0; c < CY; c++) {
           const int ry = ty + c * NTY;
-          T val = q[L - 1][c][SL];
-          if (p_int && (act_mask >> ((L - 1) * CY + c) & 1u)) {
-            const int64_t at = poff + col[c];
-            FusedAcc<R, T, QL, SL> acc{smr + ry * NTX + tx, q[L - 1][c], NTX};
-            if constexpr (TO == 2) {
-              T uold;
-              if constexpr (L >= 2) uold = q[L - 2][c][SL];
-              else uold = a.prev[at];
-              const T r2 = __ldg(a.roc2 + at);
-              if constexpr (COMP) {
-                const float lap = star_const_sum<R, FastArith>(cc, acc);
-                val = leapfrog_compensated(val, uold, r2, lap);
-              } else {
-                CoefFull<T> none{nullptr, 0};
-                val = apply_op<OP, FastArith>(cc, none, 0, acc, uold, r2);
+          T val[VX];
+#pragma unroll
+          for (int v = 0; v < VX; v++) val[v] = q[L - 1][c][v][SL];
+          if (p_int && any(L, c)) {
+            const T *srow = smr + ry * RW + tx * VX;
+            T yv[2 * R][VX];
+#pragma unroll
+            for (int d = 1; d <= R; d++) {
+              Pack<T, VX> up, dn;
+              up.load(srow + d * RW);
+              dn.load(srow - d * RW);
+#pragma unroll
+              for (int v = 0; v < VX; v++) {
+                yv[d - 1][v] = up.e[v];
+                yv[R + d - 1][v] = dn.e[v];
               }
-            } else {
-              CoefFull<T> none{nullptr, 0};
-              val = apply_op<OP, FastArith>(cc, none, 0, acc, T(0), T(0));
+            }
+            static_for<VX>([&](auto v_c) {
+              constexpr int V = decltype(v_c)::value;
+              if (bit(L, c, V)) {
+                FusedAcc<R, T, QL, SL, VX, V> acc{srow, q[L - 1][c], yv};
+                if constexpr (TO == 2) {
+                  T uold;
+                  if constexpr (L >= 2) uold = q[L - 2][c][V][SL];
+                  else uold = pvc[c].e[V];
+                  const T r2 = r2c[L & 1][c].e[V];
+                  if constexpr (COMP) {
+                    const float lap = star_const_sum<R, FastArith>(cc, acc);
+                    val[V] = leapfrog_compensated(val[V], uold, r2, lap);
+                  } else {
+                    CoefFull<T> none{nullptr, 0};
+                    val[V] = apply_op<OP, FastArith>(cc, none, 0, acc, uold, r2);
+                  }
+                } else {
+                  CoefFull<T> none{nullptr, 0};
+                  val[V] = apply_op<OP, FastArith>(cc, none, 0, acc, T(0), T(0));
+                }
+              }
+            });
+          }
+          if constexpr (L == TT || L == TT - 1) {
+            if (p_out && y_outr[c] && (L == TT || a.write_prev)) {
+              T *dst = (L == TT ? a.out_cur : a.out_prev) + poff + col[c];
+              if (x_outc[0] && x_outc[VX - 1]) {
+                Pack<T, VX> o;
+#pragma unroll
+                for (int v = 0; v < VX; v++) o.e[v] = val[v];
+                o.store(dst);
+              } else {
+#pragma unroll
+                for (int v = 0; v < VX; v++)
+                  if (x_outc[v]) dst[v] = val[v];
+              }
             }
           }
-          if (p_out && y_out[c]) {
-            if constexpr (L == TT) a.out_cur[poff + col[c]] = val;
-            if constexpr (L == TT - 1) {
-              if (a.write_prev) a.out_prev[poff + col[c]] = val;
-            }
+          if constexpr (L < TT) {
+#pragma unroll
+            for (int v = 0; v < VX; v++) q[L][c][v][SL] = val[v];
           }
-          if constexpr (L < TT) q[L][c][SL] = val;
         }
       });
       // level 0: stream plane s from HBM
       const bool s_in = s < g.nnz;
 #pragma unroll
       for (int c = 0; c < CY; c++) {
-        T v = T(0);
-        if (s_in && x_dom && y_dom[c]) v = __ldg(a.cur + soff + col[c]);
-        q[0][c][qslot<QL>(PH)] = v;
+        Pack<T, VX> in;
+#pragma unroll
+        for (int v = 0; v < VX; v++) in.e[v] = T(0);
+        if (s_in && y_dom[c]) {
+          if (xg_dom) {
+            in.ldg(a.cur + soff + col[c]);
+          } else {
+#pragma unroll
+            for (int v = 0; v < VX; v++)
+              if (x_dom[v]) in.e[v] = __ldg(a.cur + soff + col[c] + v);
+          }
+        }
+#pragma unroll
+        for (int v = 0; v < VX; v++) q[0][c][v][qslot<QL>(PH)] = in.e[v];
         if constexpr (TT == 1) {
-          if (a.write_prev && s >= R && s < g.nnz - R && s >= Z0 && s < Z1 && y_out[c])
-            a.out_prev[soff + col[c]] = v;
+          if (a.write_prev && s >= R && s < g.nnz - R && s >= Z0 && s < Z1 && y_outr[c])
+#pragma unroll
+            for (int v = 0; v < VX; v++)
+              if (x_outc[v]) a.out_prev[soff + col[c] + v] = in.e[v];
         }
       }
       // publish each level's centre plane (s - l*D - R) for the x/y neighbours of step s+1
 #pragma unroll
       for (int l = 0; l < TT; l++)
 #pragma unroll
-        for (int c = 0; c < CY; c++)
-          sm[(size_t)((wb * TT + l) * RY + ty + c * NTY) * NTX + tx] = q[l][c][qslot<QL>(PH - l * D - R)];
+        for (int c = 0; c < CY; c++) {
+          Pack<T, VX> o;
+#pragma unroll
+          for (int v = 0; v < VX; v++) o.e[v] = q[l][c][v][qslot<QL>(PH - l * D - R)];
+          o.store(sm + (size_t)((wb * TT + l) * RY + ty + c * NTY) * RW + tx * VX);
+        }
       __syncthreads();
     });
   }
 }
 
-template <int NTX, int NTY, int CY> struct VariantShape {
-  static constexpr int ntx = NTX, nty = NTY, cy = CY;
-};
-
-template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY>
+template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX>
 cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
   constexpr int R = OpTraits<OP>::R;
-  constexpr int RY = NTY * CY, H = TT * R, BX = NTX - 2 * H, BY = RY - 2 * H;
-  auto kern = fused_pass<OP, T, COMP, TT, NTX, NTY, CY>;
-  const size_t smem = (size_t)2 * TT * RY * NTX * sizeof(T);
+  constexpr int RW = NTX * VX, RY = NTY * CY, H = TT * R, BX = RW - 2 * H - (VX - 1), BY = RY - 2 * H;
+  auto kern = fused_pass<OP, T, COMP, TT, NTX, NTY, CY, VX>;
+  const size_t smem = (size_t)2 * TT * RY * RW * sizeof(T);
   static bool attr_set = false;  // per instantiation, host side
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -262,30 +376,40 @@ cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-template <int OP, class T, bool COMP, int NTX, int NTY, int CY, int TMAX>
+template <int OP, class T, bool COMP, int NTX, int NTY, int CY, int VX, int TMAX>
 cudaError_t launch_variant(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
   switch (L.steps) {
-    case 1: return launch_tt<OP, T, COMP, 1, NTX, NTY, CY>(g, L, s);
-    case 2: if constexpr (TMAX >= 2) return launch_tt<OP, T, COMP, 2, NTX, NTY, CY>(g, L, s); break;
-    case 3: if constexpr (TMAX >= 3) return launch_tt<OP, T, COMP, 3, NTX, NTY, CY>(g, L, s); break;
-    case 4: if constexpr (TMAX >= 4) return launch_tt<OP, T, COMP, 4, NTX, NTY, CY>(g, L, s); break;
-    case 5: if constexpr (TMAX >= 5) return launch_tt<OP, T, COMP, 5, NTX, NTY, CY>(g, L, s); break;
-    case 6: if constexpr (TMAX >= 6) return launch_tt<OP, T, COMP, 6, NTX, NTY, CY>(g, L, s); break;
+    case 1: return launch_tt<OP, T, COMP, 1, NTX, NTY, CY, VX>(g, L, s);
+    case 2: if constexpr (TMAX >= 2) return launch_tt<OP, T, COMP, 2, NTX, NTY, CY, VX>(g, L, s); break;
+    case 3: if constexpr (TMAX >= 3) return launch_tt<OP, T, COMP, 3, NTX, NTY, CY, VX>(g, L, s); break;
+    case 4: if constexpr (TMAX >= 4) return launch_tt<OP, T, COMP, 4, NTX, NTY, CY, VX>(g, L, s); break;
+    case 5: if constexpr (TMAX >= 5) return launch_tt<OP, T, COMP, 5, NTX, NTY, CY, VX>(g, L, s); break;
+    case 6: if constexpr (TMAX >= 6) return launch_tt<OP, T, COMP, 6, NTX, NTY, CY, VX>(g, L, s); break;
   }
   return cudaErrorInvalidValue;
 }
 
 // Maximum fusion depth instantiated per operator radius and element type.
 template <int OP, class T> constexpr int fused_tmax() {
-  return OpTraits<OP>::R == 4 ? 2 : (sizeof(T) == 8 ? 4 : 6);
+  return OpTraits<OP>::R == 4 ? 2 : (sizeof(T) == 8 ? 2 : 4);
 }
 
 template <int OP, class T, bool COMP>
 cudaError_t launch_fused_op_impl(const Geom &g, const FusedConfig &cfg, const FusedLaunch &L,
                                  cudaStream_t s) {
   constexpr int TM = fused_tmax<OP, T>();
-  if (cfg.variant == FV_64x16x2) return launch_variant<OP, T, COMP, 64, 16, 2, TM>(g, L, s);
-  return launch_variant<OP, T, COMP, 32, 16, 4, TM>(g, L, s);
+  if constexpr (OpTraits<OP>::R == 1) {  // x pairs: vector loads, stores and shared-memory traffic
+    switch (cfg.variant) {
+      case 0: return launch_variant<OP, T, COMP, 32, 16, 2, 2, TM>(g, L, s);  // 64 x 32 region, 512 threads
+      case 1: return launch_variant<OP, T, COMP, 16, 64, 1, 2, TM>(g, L, s);  // 32 x 64 region, 1024 threads
+    }
+  } else {  // radius 4: 10-plane queues leave no registers for pairs
+    switch (cfg.variant) {
+      case 0: return launch_variant<OP, T, COMP, 64, 16, 2, 1, TM>(g, L, s);  // 64 x 32 region, 1024 threads
+      case 1: return launch_variant<OP, T, COMP, 32, 32, 2, 1, TM>(g, L, s);  // 32 x 64 region, 1024 threads
+    }
+  }
+  return cudaErrorInvalidValue;
 }
 
 }  // namespace girih

@@ -16,14 +16,20 @@ pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-12
 FUSED_OPS = [1, 8, 0]
-MAX_DEPTH = {("fp64", 1): 4, ("fp64", 4): 2, ("fp32", 1): 6, ("fp32", 4): 2, ("mixed", 1): 6, ("mixed", 4): 2}
-TILE = {0: (64, 32), 1: (32, 64)}  # column region of the two CTA variants
+MAX_DEPTH = {("fp64", 1): 2, ("fp64", 4): 2, ("fp32", 1): 4, ("fp32", 4): 2, ("mixed", 1): 4, ("mixed", 4): 2}
+TILE = {0: (64, 32), 1: (32, 64)}  # column region of the CTA variants
+SMEM_MAX = 227 * 1024
 
 
 def _block(op, depth, variant):
     r = gpu.OP_INFO[op][0]
     w, h = TILE[variant]
-    return (w - 2 * depth * r, h - 2 * depth * r)
+    return (w - 2 * depth * r - (1 if r == 1 else 0), h - 2 * depth * r)  # x pairs lose one column
+
+
+def _fits(variant, depth, tsz):
+    w, h = TILE[variant]
+    return 2 * depth * w * h * tsz <= SMEM_MAX
 
 
 def _shape(op):
@@ -38,6 +44,10 @@ def test_fused_fp64_all_depths(op, variant):
     nt = 9
     ref = g0.copy().run(nt, nthreads=4)
     for depth in range(1, MAX_DEPTH[("fp64", r)] + 1):
+        if not _fits(variant, depth, 8):
+            with pytest.raises(gpu.GirihGpuError):
+                gpu.Context(op, *_shape(op), schedule="fused", fusion_depth=depth, block=_block(op, depth, variant))
+            continue
         g = g0.copy()
         with gpu_context(g, precision="fp64", schedule="fused", fusion_depth=depth,
                          block=_block(op, depth, variant)) as ctx:

@@ -104,6 +104,15 @@ __device__ __forceinline__ float leapfrog_compensated(float v, float u, float r2
 
 __device__ __forceinline__ int pmod(int a, int m) { return ((a % m) + m) % m; }
 
+// Hint that a global line will be read soon: fetch it into L2 without holding
+// a register (the z streams touch every HBM line for the first time here).
+__device__ __forceinline__ void prefetch_l2(const void *p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// distance, in z planes, of the L2 prefetch ahead of the plane being loaded
+constexpr int kPrefetchPlanes = 6;
+
 template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX>
 __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
   constexpr int R = OpTraits<OP>::R;
@@ -282,6 +291,29 @@ __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
           }
         }
       });
+      // L2 prefetch of the planes this thread will load a few steps from now:
+      // the input state at s + kPrefetchPlanes, and roc2 / the old state at the
+      // plane level 1 reaches then
+      {
+        const int sp = s + kPrefetchPlanes;
+        if (sp < g.nnz && xg_dom) {
+#pragma unroll
+          for (int c = 0; c < CY; c++)
+            if (y_dom[c]) prefetch_l2(a.cur + (int64_t)sp * plane + col[c]);
+        }
+        if constexpr (TO == 2) {
+          const int pp = sp - D;
+          if (pp >= R && pp < g.nnz - R) {
+#pragma unroll
+            for (int c = 0; c < CY; c++)
+              if (any(1, c)) {
+                const int64_t at = (int64_t)pp * plane + col[c];
+                prefetch_l2(a.roc2 + at);
+                prefetch_l2(a.prev + at);
+              }
+          }
+        }
+      }
       // level 0: stream plane s from HBM
       const bool s_in = s < g.nnz;
 #pragma unroll

@@ -32,9 +32,10 @@ FusedConfig make_fused_config(const Geom &g, int precision, int depth, int varia
     return c;
   int ntx, ry, vx;
   variant_shape(variant, g.r, &ntx, &ry, &vx);
-  // double-buffered shared memory of all levels must fit one CTA (227 KiB)
+  // double-buffered shared memory of all levels (rows padded by r) must fit one CTA (227 KiB)
   const size_t tsz = precision == GIRIH_FP64 ? 8 : 4;
-  if ((size_t)2 * depth * ntx * ry * tsz > (size_t)227 * 1024) return c;
+  const int rp = (g.r + vx - 1) / vx * vx;
+  if ((size_t)2 * depth * (ntx + 2 * rp) * (ry + 2 * g.r) * tsz > (size_t)227 * 1024) return c;
   c.depth = depth;
   c.variant = variant;
   c.bx = ntx - 2 * depth * g.r - (vx - 1);  // pairs lose one column to their alignment

@@ -104,31 +104,35 @@ __device__ __forceinline__ float leapfrog_compensated(float v, float u, float r2
 
 __device__ __forceinline__ int pmod(int a, int m) { return ((a % m) + m) % m; }
 
-// Hint that a global line will be read soon: fetch it into L2 without holding
-// a register (the z streams touch every HBM line for the first time here).
-__device__ __forceinline__ void prefetch_l2(const void *p) {
-  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-}
 
-// distance, in z planes, of the L2 prefetch ahead of the plane being loaded
-constexpr int kPrefetchPlanes = 6;
+template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX>
+struct FusedShape {
+  static constexpr int R = OpTraits<OP>::R;
+  static constexpr int TO = OpTraits<OP>::TO;
+  static constexpr int D = R + 1;                            // planes between time levels
+  static constexpr int QL = TO == 2 ? 2 * R + 2 : 2 * R + 1;  // z-queue length
+  static constexpr int U = QL % 2 == 0 ? QL : 2 * QL;         // z-loop unroll: even multiple of QL
+  static constexpr int RW = NTX * VX, RY = NTY * CY;          // column region
+  static constexpr int RP = (R + VX - 1) / VX * VX;           // column padding, a whole number of x groups
+  static constexpr int PW = RW + 2 * RP, PR = RY + 2 * R;     // shared rows padded by RP, rows by R
+  static constexpr int H = TT * R;
+  static constexpr int BX = RW - 2 * H - (VX - 1), BY = RY - 2 * H;  // output tile
+  static constexpr size_t smem_bytes = (size_t)2 * TT * PR * PW * sizeof(T);
+};
 
 template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX>
 __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
-  constexpr int R = OpTraits<OP>::R;
-  constexpr int TO = OpTraits<OP>::TO;
-  constexpr int D = R + 1;
-  constexpr int QL = TO == 2 ? 2 * R + 2 : 2 * R + 1;
-  constexpr int RW = NTX * VX;  // region width (columns)
-  constexpr int RY = NTY * CY;  // region height (rows)
-  constexpr int H = TT * R;
-  constexpr int BX = RW - 2 * H - (VX - 1);
-  constexpr int BY = RY - 2 * H;
+  using S = FusedShape<OP, T, COMP, TT, NTX, NTY, CY, VX>;
+  constexpr int R = S::R, TO = S::TO, D = S::D, QL = S::QL, U = S::U;
+  constexpr int RW = S::RW, RY = S::RY, RP = S::RP, PW = S::PW, PR = S::PR, H = S::H, BX = S::BX, BY = S::BY;
+  static_assert(PW % VX == 0 && RP % VX == 0, "x groups must stay vector-aligned in shared memory");
   static_assert(BX > 0 && BY > 0, "tile too small for the fusion depth");
   static_assert(TT * CY * VX <= 32, "activity mask holds 32 (level, row, column) bits");
 
   extern __shared__ __align__(16) unsigned char smraw[];
-  T *sm = reinterpret_cast<T *>(smraw);  // [2][TT][RY][RW]
+  // [2 buffers][TT levels][PR rows][PW columns]; the padding is never written and
+  // only feeds values that are discarded, so every neighbour read stays in bounds
+  T *sm = reinterpret_cast<T *>(smraw);
 
   const Geom &g = a.g;
   const int64_t plane = g.plane;
@@ -138,7 +142,7 @@ __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
   const int Z1 = min(Z0 + a.zchunk, g.nnz - R);
   const int sb = max(0, Z0 - H);
   const int se = Z1 - 1 + TT * D;
-  const int s0 = sb - sb % QL;  // aligned so that plane p lives in slot p mod QL
+  const int s0 = sb - sb % U;  // plane p lives in queue slot p mod QL; buffer parity = PH parity
 
   // region start, aligned so that every thread's x-group is one aligned vector in memory
   const int xs = X0 - H - pmod(X0 - H + R + g.ox, VX);
@@ -175,8 +179,6 @@ __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
         for (int v = 0; v < VX; v++)
           if (x_act >> ((l - 1) * VX + v) & 1u) act |= 1u << (((l - 1) * CY + c) * VX + v);
   }
-  auto bit = [&](int l, int c, int v) -> bool { return act >> (((l - 1) * CY + c) * VX + v) & 1u; };
-  auto any = [&](int l, int c) -> bool { return (act >> (((l - 1) * CY + c) * VX)) & ((1u << VX) - 1); };
 
   T cc[5];
 #pragma unroll
@@ -192,30 +194,42 @@ __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
 #pragma unroll
         for (int e = 0; e < QL; e++) q[l][c][v][e] = T(0);
 
-  for (int sbase = s0; sbase <= se; sbase += QL) {
-    static_for<QL>([&](auto ph_c) {
+  // shared-memory element of this thread's first column, row c, level l, buffer b:
+  //   sm + thr + ((b*TT + l)*PR + c*NTY)*PW   (compile-time offsets from thr)
+  T *const thr = sm + (ty + R) * PW + tx * VX + RP;
+
+  for (int sbase = s0; sbase <= se; sbase += U) {
+    static_for<U>([&](auto ph_c) {
       constexpr int PH = decltype(ph_c)::value;
+      constexpr int RB = (PH + 1) & 1, WB = PH & 1;  // read buffer (s-1) and write buffer (s)
       const int s = sbase + PH;
       if (s > se) return;  // uniform over the CTA
-      const int rb = (s - 1) & 1, wb = s & 1;
       const int64_t soff = (int64_t)s * plane;
-      // roc2 (and, for level 1, the old state) of level l are loaded while level
-      // l+1 computes: two levels' worth of registers, latency overlapped
-      Pack<T, VX> r2c[2][CY], pvc[CY];
-      auto issue = [&](int l) {
-        if constexpr (TO == 2) {
+
+      // roc2 (and, for level 1, the old state) of every level, issued before the
+      // level loop so that their latency overlaps the higher levels' arithmetic
+      Pack<T, VX> r2c[TO == 2 ? TT : 1][CY], pvc[CY];
+      if constexpr (TO == 2) {
+#pragma unroll
+        for (int l = TT; l >= 1; l--) {
           const int p = s - l * D;
           const bool p_int = p >= R && p < g.nnz - R;
 #pragma unroll
-          for (int c = 0; c < CY; c++)
-            if (p_int && any(l, c)) {
-              const int64_t at = (int64_t)p * plane + col[c];
-              r2c[l & 1][c].ldg(a.roc2 + at);
+          for (int c = 0; c < CY; c++) {
+            const int64_t at = (int64_t)p * plane + col[c];
+#pragma unroll
+            for (int v = 0; v < VX; v++) r2c[l - 1][c].e[v] = T(0);
+            if (l == 1)
+#pragma unroll
+              for (int v = 0; v < VX; v++) pvc[c].e[v] = T(0);
+            if (p_int && ((act >> (((l - 1) * CY + c) * VX)) & ((1u << VX) - 1))) {
+              r2c[l - 1][c].ldg(a.roc2 + at);
               if (l == 1) pvc[c].ldg(a.prev + at);
             }
+          }
         }
-      };
-      issue(TT);
+      }
+
       // levels TT..1, highest first: level l reads level l-1's queues before
       // level l-1 stores this step's plane
       static_for<TT>([&](auto li_c) {
@@ -225,51 +239,45 @@ __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
         const bool p_int = p >= R && p < g.nnz - R;
         const bool p_out = p_int && p >= Z0 && p < Z1;
         const int64_t poff = soff - (int64_t)(L * D) * plane;
-        const T *smr = sm + (size_t)((rb * TT + (L - 1)) * RY) * RW;
-        if constexpr (L > 1) issue(L - 1);
 #pragma unroll
         for (int c = 0; c < CY; c++) {
-          const int ry = ty + c * NTY;
-          T val[VX];
+          const T *srow = thr + ((RB * TT + (L - 1)) * PR + c * NTY) * PW;
+          T yv[2 * R][VX];
 #pragma unroll
-          for (int v = 0; v < VX; v++) val[v] = q[L - 1][c][v][SL];
-          if (p_int && any(L, c)) {
-            const T *srow = smr + ry * RW + tx * VX;
-            T yv[2 * R][VX];
+          for (int d = 1; d <= R; d++) {
+            Pack<T, VX> up, dn;
+            up.load(srow + d * PW);
+            dn.load(srow - d * PW);
 #pragma unroll
-            for (int d = 1; d <= R; d++) {
-              Pack<T, VX> up, dn;
-              up.load(srow + d * RW);
-              dn.load(srow - d * RW);
-#pragma unroll
-              for (int v = 0; v < VX; v++) {
-                yv[d - 1][v] = up.e[v];
-                yv[R + d - 1][v] = dn.e[v];
-              }
+            for (int v = 0; v < VX; v++) {
+              yv[d - 1][v] = up.e[v];
+              yv[R + d - 1][v] = dn.e[v];
             }
-            static_for<VX>([&](auto v_c) {
-              constexpr int V = decltype(v_c)::value;
-              if (bit(L, c, V)) {
-                FusedAcc<R, T, QL, SL, VX, V> acc{srow, q[L - 1][c], yv};
-                if constexpr (TO == 2) {
-                  T uold;
-                  if constexpr (L >= 2) uold = q[L - 2][c][V][SL];
-                  else uold = pvc[c].e[V];
-                  const T r2 = r2c[L & 1][c].e[V];
-                  if constexpr (COMP) {
-                    const float lap = star_const_sum<R, FastArith>(cc, acc);
-                    val[V] = leapfrog_compensated(val[V], uold, r2, lap);
-                  } else {
-                    CoefFull<T> none{nullptr, 0};
-                    val[V] = apply_op<OP, FastArith>(cc, none, 0, acc, uold, r2);
-                  }
-                } else {
-                  CoefFull<T> none{nullptr, 0};
-                  val[V] = apply_op<OP, FastArith>(cc, none, 0, acc, T(0), T(0));
-                }
-              }
-            });
           }
+          T val[VX];
+          static_for<VX>([&](auto v_c) {
+            constexpr int V = decltype(v_c)::value;
+            const T centre = q[L - 1][c][V][SL];
+            FusedAcc<R, T, QL, SL, VX, V> acc{srow, q[L - 1][c], yv};
+            T cand;
+            if constexpr (TO == 2) {
+              T uold;
+              if constexpr (L >= 2) uold = q[L - 2][c][V][SL];
+              else uold = pvc[c].e[V];
+              const T r2 = r2c[L - 1][c].e[V];
+              if constexpr (COMP) {
+                cand = leapfrog_compensated(centre, uold, r2, star_const_sum<R, FastArith>(cc, acc));
+              } else {
+                CoefFull<T> none{nullptr, 0};
+                cand = apply_op<OP, FastArith>(cc, none, 0, acc, uold, r2);
+              }
+            } else {
+              CoefFull<T> none{nullptr, 0};
+              cand = apply_op<OP, FastArith>(cc, none, 0, acc, T(0), T(0));
+            }
+            const bool on = p_int && (act >> (((L - 1) * CY + c) * VX + V) & 1u);
+            val[V] = on ? cand : centre;  // halo and out-of-region points keep their value
+          });
           if constexpr (L == TT || L == TT - 1) {
             if (p_out && y_outr[c] && (L == TT || a.write_prev)) {
               T *dst = (L == TT ? a.out_cur : a.out_prev) + poff + col[c];
@@ -291,29 +299,6 @@ __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
           }
         }
       });
-      // L2 prefetch of the planes this thread will load a few steps from now:
-      // the input state at s + kPrefetchPlanes, and roc2 / the old state at the
-      // plane level 1 reaches then
-      {
-        const int sp = s + kPrefetchPlanes;
-        if (sp < g.nnz && xg_dom) {
-#pragma unroll
-          for (int c = 0; c < CY; c++)
-            if (y_dom[c]) prefetch_l2(a.cur + (int64_t)sp * plane + col[c]);
-        }
-        if constexpr (TO == 2) {
-          const int pp = sp - D;
-          if (pp >= R && pp < g.nnz - R) {
-#pragma unroll
-            for (int c = 0; c < CY; c++)
-              if (any(1, c)) {
-                const int64_t at = (int64_t)pp * plane + col[c];
-                prefetch_l2(a.roc2 + at);
-                prefetch_l2(a.prev + at);
-              }
-          }
-        }
-      }
       // level 0: stream plane s from HBM
       const bool s_in = s < g.nnz;
 #pragma unroll
@@ -347,7 +332,7 @@ __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
           Pack<T, VX> o;
 #pragma unroll
           for (int v = 0; v < VX; v++) o.e[v] = q[l][c][v][qslot<QL>(PH - l * D - R)];
-          o.store(sm + (size_t)((wb * TT + l) * RY + ty + c * NTY) * RW + tx * VX);
+          o.store(thr + ((WB * TT + l) * PR + c * NTY) * PW);
         }
       __syncthreads();
     });
@@ -356,10 +341,10 @@ __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
 
 template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX>
 cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
-  constexpr int R = OpTraits<OP>::R;
-  constexpr int RW = NTX * VX, RY = NTY * CY, H = TT * R, BX = RW - 2 * H - (VX - 1), BY = RY - 2 * H;
+  using S = FusedShape<OP, T, COMP, TT, NTX, NTY, CY, VX>;
+  constexpr int R = S::R, BX = S::BX, BY = S::BY;
   auto kern = fused_pass<OP, T, COMP, TT, NTX, NTY, CY, VX>;
-  const size_t smem = (size_t)2 * TT * RY * RW * sizeof(T);
+  const size_t smem = S::smem_bytes;
   static bool attr_set = false;  // per instantiation, host side
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

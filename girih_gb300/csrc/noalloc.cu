@@ -103,6 +103,13 @@ extern "C" int girih_gpu_fused_run_noalloc(const girih_gpu_desc *d, void *U1, vo
   if (d->device < 0 || d->device >= kMaxDevices) return fail_na(GIRIH_GPU_EINVAL, "device ordinal out of range");
 
   const int tsz = d->precision == GIRIH_FP64 ? 8 : 4;
+  // the radius-1 fused kernels move x pairs as one vector: rows must start on
+  // a pair boundary and the arrays on a 16-byte boundary
+  if (d->ldomain_shape[0] % 2 != 0)
+    return fail_na(GIRIH_GPU_EINVAL, "ldomain_shape[0] (x pitch) must be even for the no-allocation entry point");
+  for (const void *ptr : {(const void *)U1, (const void *)U2, U3})
+    if (ptr && (reinterpret_cast<uintptr_t>(ptr) & 15u))
+      return fail_na(GIRIH_GPU_EINVAL, "device arrays must be 16-byte aligned");
   const Geom g = reference_layout_geom(d);
   const size_t state_bytes = (size_t)g.elems * tsz;
   const size_t spare_bytes = (state_bytes + 255) / 256 * 256;

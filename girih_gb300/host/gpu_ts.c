@@ -1,0 +1,102 @@
+/*
+ * GPU time stepper for the girih driver: the entry
+ *     {"GPU (libgirih_gpu)", gpu_ts}
+ * of the time-stepper table (reference: struct time_stepper,
+ * src/data_structures.h:412-415; table src/wrappers.h:28-36).  It has the
+ * signature of every reference stepper, void (*)(Parameters *), and is called
+ * the same way: by the performance harness inside its MPI_Wtime bracket
+ * (src/performance.c:74-78) and by the verifier (src/verification.c:37), which
+ * then compares p->U1 with the serial reference operators.
+ *
+ * Each call advances p->U1/p->U2 by nt steps exactly like
+ * naive_nonblocking_ts (src/kernels/nb_naive_ts.c:187-203): the host arrays are
+ * copied to the GPU, the time loop runs there, and U1 (state nt-1) and U2
+ * (state nt) are copied back.  The reference CLI has no precision or schedule
+ * options, so they come from the environment:
+ *   GIRIH_GPU_PRECISION = fp64 (default) | fp32 | mixed
+ *   GIRIH_GPU_SCHEDULE  = plain (default) | fused | auto
+ *   GIRIH_GPU_EXACT     = 1 (default for fp64 plain: the serial reference's rounding,
+ *                         so --verify 1 passes its bit-exact check) | 0
+ *   GIRIH_GPU_DEVICE    = CUDA device ordinal (default 0)
+ * Errors are reported through the reference's RAISE_ERROR.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "data_structures.h"
+#include "girih_gpu.h"
+
+static girih_gpu_ctx *g_ctx = NULL;
+static girih_gpu_desc g_desc;
+
+static int env_choice(const char *name, const char *const *names, int n, int def) {
+  const char *v = getenv(name);
+  if (!v || !*v) return def;
+  for (int i = 0; i < n; i++)
+    if (strcmp(v, names[i]) == 0) return i;
+  fprintf(stderr, "ERROR: %s=%s is not one of the accepted values\n", name, v);
+  exit(1);
+}
+
+static void gpu_ts_release(void) {
+  if (g_ctx) girih_gpu_destroy(g_ctx);
+  g_ctx = NULL;
+}
+
+static void gpu_ts_fail(Parameters *p, const char *what, int err) {
+  if (p->mpi_rank == 0)
+    fprintf(stderr, "ERROR: %s: %s (%s)\n", what, girih_gpu_strerror(err), girih_gpu_last_error());
+  gpu_ts_release();
+  RAISE_ERROR("GPU time stepper failed");
+}
+
+void gpu_ts(Parameters *p) {
+  static const char *const precisions[] = {"fp64", "fp32", "mixed"};
+  static const char *const schedules[] = {"plain", "fused", "auto"};
+  if (p->mpi_size != 1) RAISE_ERROR("the GPU time stepper runs one grid per process: use a single rank");
+  if (p->stencil.type != REGULAR || p->stencil.shape != STAR)
+    RAISE_ERROR("the GPU time stepper provides the star operators only");
+
+  girih_gpu_desc d;
+  memset(&d, 0, sizeof(d));
+  d.target_kernel = p->target_kernel;
+  for (int i = 0; i < 3; i++) {
+    d.stencil_shape[i] = p->lstencil_shape[i];
+    d.ldomain_shape[i] = p->ldomain_shape[i];
+  }
+  d.host_real_size = (int)sizeof(real_t);
+  d.precision = env_choice("GIRIH_GPU_PRECISION", precisions, 3, GIRIH_FP64);
+  d.schedule = env_choice("GIRIH_GPU_SCHEDULE", schedules, 3, GIRIH_SCHED_PLAIN);
+  const char *ex = getenv("GIRIH_GPU_EXACT");
+  d.exact = ex ? atoi(ex) != 0 : (d.precision == GIRIH_FP64 && d.schedule == GIRIH_SCHED_PLAIN);
+  const char *dev = getenv("GIRIH_GPU_DEVICE");
+  d.device = dev ? atoi(dev) : 0;
+
+  if (g_ctx && memcmp(&d, &g_desc, sizeof(d)) != 0) gpu_ts_release();
+  int e;
+  if (!g_ctx) {
+    if ((e = girih_gpu_create(&g_ctx, &d))) {
+      g_ctx = NULL;
+      gpu_ts_fail(p, "girih_gpu_create", e);
+    }
+    g_desc = d;
+    atexit(gpu_ts_release);
+  }
+  if ((e = girih_gpu_upload(g_ctx, p->U1, p->U2, p->U3, p->coef))) gpu_ts_fail(p, "girih_gpu_upload", e);
+  float ms = 0.f;
+  if ((e = girih_gpu_run(g_ctx, p->nt, &ms))) gpu_ts_fail(p, "girih_gpu_run", e);
+  if ((e = girih_gpu_download(g_ctx, p->U1, p->U2))) gpu_ts_fail(p, "girih_gpu_download", e);
+
+  /* the device time of the loop is the stepper's compute time
+   * (the reference accumulates it the same way, nb_naive_ts.c:205-206) */
+  p->prof.compute += ms * 1e-3;
+  if (p->verbose && p->mpi_rank == 0) {
+    girih_gpu_info_t info;
+    girih_gpu_info(g_ctx, &info);
+    int steps = 2 * ((p->nt + 1) / 2);
+    printf("GPU stepper: %s %s depth %d, %d launches, device time %.3f ms, %.3f GLUP/s (device only)\n",
+           precisions[info.precision], schedules[info.schedule], info.fusion_depth, info.launches_last_run, ms,
+           ms > 0 ? (double)p->ln_stencils * steps / (ms * 1e6) : 0.0);
+  }
+}

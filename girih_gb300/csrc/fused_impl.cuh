@@ -120,8 +120,12 @@ struct FusedShape {
   static constexpr size_t smem_bytes = (size_t)2 * TT * PR * PW * sizeof(T);
 };
 
+// One CTA-tile of a fused pass: tile (bxi, byi) of the x-y tiling, z chunk bzi,
+// executed by the NTX*NTY threads of the calling CTA (thread (tx, ty)).  Used by
+// the single-grid kernel below and by the batched persistent kernel.
 template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX>
-__global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
+__device__ __forceinline__ void fused_tile(const FusedArgs<T> &a, int bxi, int byi, int bzi, int tx, int ty,
+                                           unsigned char *smraw) {
   using S = FusedShape<OP, T, COMP, TT, NTX, NTY, CY, VX>;
   constexpr int R = S::R, TO = S::TO, D = S::D, QL = S::QL, U = S::U;
   constexpr int RW = S::RW, RY = S::RY, RP = S::RP, PW = S::PW, PR = S::PR, H = S::H, BX = S::BX, BY = S::BY;
@@ -129,16 +133,14 @@ __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
   static_assert(BX > 0 && BY > 0, "tile too small for the fusion depth");
   static_assert(TT * CY * VX <= 32, "activity mask holds 32 (level, row, column) bits");
 
-  extern __shared__ __align__(16) unsigned char smraw[];
   // [2 buffers][TT levels][PR rows][PW columns]; the padding is never written and
   // only feeds values that are discarded, so every neighbour read stays in bounds
   T *sm = reinterpret_cast<T *>(smraw);
 
   const Geom &g = a.g;
   const int64_t plane = g.plane;
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int X0 = blockIdx.x * BX, Y0 = blockIdx.y * BY;
-  const int Z0 = R + blockIdx.z * a.zchunk;
+  const int X0 = bxi * BX, Y0 = byi * BY;
+  const int Z0 = R + bzi * a.zchunk;
   const int Z1 = min(Z0 + a.zchunk, g.nnz - R);
   const int sb = max(0, Z0 - H);
   const int se = Z1 - 1 + TT * D;
@@ -337,6 +339,13 @@ __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
       __syncthreads();
     });
   }
+}
+
+template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX>
+__global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  fused_tile<OP, T, COMP, TT, NTX, NTY, CY, VX>(a, blockIdx.x, blockIdx.y, blockIdx.z, threadIdx.x, threadIdx.y,
+                                                smraw);
 }
 
 template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX>

@@ -61,32 +61,7 @@ Geom make_geom(int op, int nx, int ny, int nz, int hpx, int tsz) {
 
 using namespace girih;
 
-struct girih_gpu_ctx {
-  girih_gpu_desc d{};
-  Geom g{};
-  int tsz = 8, hsz = 8;
-  bool bf16coef = false;
-  cudaStream_t st = nullptr;
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
-  void *f[4] = {nullptr, nullptr, nullptr, nullptr};  // field buffers
-  int iu1 = 0, iu2 = 1;                               // buffers holding U1 and U2
-  void *roc2 = nullptr;
-  void *coef = nullptr;
-  float *scale = nullptr;
-  double cc[5] = {0, 0, 0, 0, 0};
-  void *staging = nullptr;
-  size_t staging_bytes = 0;
-  double *acc = nullptr;  // 4 doubles for norms, then flag words
-  bool uploaded = false;
-  bool halos_equal = false;
-  int sched = GIRIH_SCHED_PLAIN;
-  FusedConfig fcfg{};
-  cudaGraphExec_t gexec = nullptr;
-  int g_steps = -1, g_iu1 = -1, g_iu2 = -1;
-  int g_launches = 0, g_new_iu1 = 0, g_new_iu2 = 1;
-  int last_launches = 0, last_steps = 0;
-  double dev_bytes = 0;
-};
+#include "context.cuh"
 
 namespace {
 
@@ -271,7 +246,7 @@ template <class T> StepArgs<T> step_args(girih_gpu_ctx *c, void *u, const void *
 // into a graph by the caller).  Plain: U1 <- op(U2), U2 <- op(U1) in place of
 // the reference's two sweeps per iteration.  Fused: passes of depth T rotate
 // through the four field buffers.
-int issue_steps(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *iu2) {
+int issue_steps_impl(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *iu2, cudaStream_t st) {
   *launches = 0;
   const bool exact = c->d.exact != 0;
   if (c->sched == GIRIH_SCHED_PLAIN) {
@@ -279,8 +254,8 @@ int issue_steps(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *iu2) 
       for (int h = 0; h < 2; h++) {
         void *u = c->f[h == 0 ? *iu1 : *iu2];
         const void *v = c->f[h == 0 ? *iu2 : *iu1];
-        cudaError_t e = c->tsz == 8 ? launch_plain<double>(step_args<double>(c, u, v), exact, false, c->st)
-                                    : launch_plain<float>(step_args<float>(c, u, v), exact, c->bf16coef, c->st);
+        cudaError_t e = c->tsz == 8 ? launch_plain<double>(step_args<double>(c, u, v), exact, false, st)
+                                    : launch_plain<float>(step_args<float>(c, u, v), exact, c->bf16coef, st);
         if (e != cudaSuccess) return fail(GIRIH_GPU_ECUDA, std::string("plain launch: ") + cudaGetErrorString(e));
         (*launches)++;
       }
@@ -305,7 +280,7 @@ int issue_steps(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *iu2) 
     // time order 1 never reads state t-1, so only the last pass writes it (U1)
     L.write_prev = (c->g.to == 2 || left == T) ? 1 : 0;
     for (int m = 0; m < 5; m++) L.cc[m] = c->cc[m];
-    cudaError_t e = launch_fused(c->g, c->tsz, c->d.precision, c->fcfg, L, c->st);
+    cudaError_t e = launch_fused(c->g, c->tsz, c->d.precision, c->fcfg, L, st);
     if (e != cudaSuccess) return fail(GIRIH_GPU_ECUDA, std::string("fused launch: ") + cudaGetErrorString(e));
     (*launches)++;
     *iu1 = spare[0];
@@ -315,7 +290,18 @@ int issue_steps(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *iu2) 
   return 0;
 }
 
+int issue_steps(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *iu2) {
+  return issue_steps_impl(c, steps, launches, iu1, iu2, c->st);
+}
+
 }  // namespace
+
+namespace girih {
+int issue_steps_on(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *iu2, cudaStream_t st) {
+  return issue_steps_impl(c, steps, launches, iu1, iu2, st);
+}
+int ensure_fused_buffers_pub(girih_gpu_ctx *c) { return ensure_fused_buffers(c); }
+}  // namespace girih
 
 extern "C" {
 

@@ -76,6 +76,16 @@ def lib():
                                                   ctypes.c_int, P]
         L.girih_gpu_info.argtypes = [P, ctypes.POINTER(Info)]
         L.girih_gpu_autotune.argtypes = [P, ctypes.c_int, ctypes.POINTER(Info)]
+        L.girih_gpu_batch_create.argtypes = [ctypes.POINTER(P), ctypes.c_int, ctypes.POINTER(Desc)]
+        L.girih_gpu_batch_destroy.argtypes = [P]
+        L.girih_gpu_batch_destroy.restype = None
+        L.girih_gpu_batch_grid.argtypes = [P, ctypes.c_int]
+        L.girih_gpu_batch_grid.restype = P
+        L.girih_gpu_batch_autotune.argtypes = [P, ctypes.c_int]
+        L.girih_gpu_batch_run.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
+        L.girih_gpu_batch_run_looped.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
+        L.girih_gpu_batch_info.argtypes = [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                           ctypes.POINTER(ctypes.c_int)]
         L.girih_gpu_strerror.argtypes = [ctypes.c_int]
         L.girih_gpu_strerror.restype = ctypes.c_char_p
         L.girih_gpu_last_error.restype = ctypes.c_char_p
@@ -201,6 +211,84 @@ class Context:
         inf = Info()
         _check(lib().girih_gpu_info(self._h, ctypes.byref(inf)), "girih_gpu_info")
         return {k: (getattr(inf, k).decode() if k == "kernel_name" else getattr(inf, k)) for k, _ in Info._fields_}
+
+
+class _GridView(Context):
+    """A grid owned by a Batch: the single-grid calls on its context, no ownership."""
+
+    def __init__(self, handle, op, nx, ny, nz, pnx, precision):
+        r = OP_INFO[op][0]
+        self.op, self.r = op, r
+        self.nx, self.ny, self.nz, self.pnx = nx, ny, nz, pnx
+        self.host_dtype = np.float64
+        self._h = ctypes.c_void_p(handle)
+
+    def close(self):
+        self._h = ctypes.c_void_p()  # the batch destroys its grids
+
+
+class Batch:
+    """Many grids advanced together by the persistent batched kernel."""
+
+    def __init__(self, grids, precision="mixed", device=0):
+        """grids: list of (op, nx, ny, nz)."""
+        n = len(grids)
+        descs = (Desc * n)()
+        self.views = []
+        for k, (op, nx, ny, nz) in enumerate(grids):
+            r = OP_INFO[op][0]
+            d = descs[k]
+            d.target_kernel = op
+            d.stencil_shape[:] = [nx, ny, nz]
+            d.ldomain_shape[:] = [padded_nx(nx, r), ny + 2 * r, nz + 2 * r]
+            d.host_real_size = 8
+            d.precision = PRECISIONS[precision]
+            d.schedule = FUSED
+            d.device = device
+        self._h = ctypes.c_void_p()
+        _check(lib().girih_gpu_batch_create(ctypes.byref(self._h), n, descs), "girih_gpu_batch_create")
+        for k, (op, nx, ny, nz) in enumerate(grids):
+            hnd = lib().girih_gpu_batch_grid(self._h, k)
+            self.views.append(_GridView(hnd, op, nx, ny, nz, padded_nx(nx, OP_INFO[op][0]), precision))
+
+    def grid(self, k):
+        return self.views[k]
+
+    def autotune(self, trial_steps=0):
+        _check(lib().girih_gpu_batch_autotune(self._h, trial_steps), "girih_gpu_batch_autotune")
+
+    def run(self, nt):
+        ms = ctypes.c_float()
+        _check(lib().girih_gpu_batch_run(self._h, nt, ctypes.byref(ms)), "girih_gpu_batch_run")
+        return ms.value
+
+    def run_looped(self, nt):
+        ms = ctypes.c_float()
+        _check(lib().girih_gpu_batch_run_looped(self._h, nt, ctypes.byref(ms)), "girih_gpu_batch_run_looped")
+        return ms.value
+
+    def info(self):
+        la, it = ctypes.c_int(), ctypes.c_int()
+        dep = (ctypes.c_int * len(self.views))()
+        _check(lib().girih_gpu_batch_info(self._h, ctypes.byref(la), ctypes.byref(it), dep), "girih_gpu_batch_info")
+        return {"launches_last_run": la.value, "items_last_run": it.value, "depths": list(dep)}
+
+    def close(self):
+        if self._h:
+            lib().girih_gpu_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def fused_run_noalloc(op, nx, ny, nz, U1, U2, U3, coefs, nt, precision="fp64", pnx=None, fusion_depth=0,

@@ -174,6 +174,27 @@ int girih_gpu_autotune(girih_gpu_ctx *c, int trial_steps, girih_gpu_info_t *chos
 int girih_gpu_fused_run_noalloc(const girih_gpu_desc *d, void *U1, void *U2, const void *U3,
                                 const double *coefs, int nt, void *stream);
 
+/* Batched time stepping (no counterpart in the reference, which advances one
+ * grid per process): n independent grids of any sizes, operators 0, 1 and 8,
+ * one precision and one device, advanced together by one persistent kernel
+ * launch per fused pass that pulls (grid, tile, z chunk) work items from an
+ * atomic counter, largest first; the whole time loop is a captured CUDA graph.
+ * Each grid is an ordinary context: girih_gpu_batch_grid() returns it for
+ * upload / fill_seeded / download / norms. */
+typedef struct girih_gpu_batch girih_gpu_batch;
+int girih_gpu_batch_create(girih_gpu_batch **out, int n, const girih_gpu_desc *descs);
+void girih_gpu_batch_destroy(girih_gpu_batch *b);
+girih_gpu_ctx *girih_gpu_batch_grid(girih_gpu_batch *b, int g);
+/* Fusion depth per (operator, size class), timed on one grid of each class;
+ * grid states are restored. */
+int girih_gpu_batch_autotune(girih_gpu_batch *b, int trial_steps);
+/* Advance every grid like girih_gpu_run(); *ms_out = device time of the loop. */
+int girih_gpu_batch_run(girih_gpu_batch *b, int nt, float *ms_out);
+/* The same steps with each grid's own single-grid kernels, one grid after the
+ * other (the comparison baseline), also graph-replayed. */
+int girih_gpu_batch_run_looped(girih_gpu_batch *b, int nt, float *ms_out);
+int girih_gpu_batch_info(girih_gpu_batch *b, int *launches_last_run, int *items_last_run, int *depths);
+
 const char *girih_gpu_strerror(int err);
 const char *girih_gpu_last_error(void); /* detail of the calling thread's last error */
 int girih_gpu_abi_version(void);

@@ -282,6 +282,80 @@ def run_ours(args, wl, rank, world, local):
     return line
 
 
+def batched_grids(seed=4, n=64):
+    """64 grids: edges from {32,48,64,96,128,160,192}, cubes and 2:1:1 boxes,
+    half the 7-point leapfrog (operator 8), half the 25-point leapfrog (operator 0)."""
+    import numpy as np
+    rng = np.random.Generator(np.random.PCG64(seed))
+    edges = [32, 48, 64, 96, 128, 160, 192]
+    grids = []
+    for k in range(n):
+        e = int(rng.choice(edges))
+        op = 8 if k < n // 2 else 0
+        if k % 2 == 0:
+            grids.append((op, e, e, e))
+        else:
+            grids.append((op, e, max(8, e // 2), max(8, e // 2)))
+    return grids
+
+
+BATCH_INPUTS = {8: dict(f=(0.0, 1.0), roc2=(0.5, 1.5), coefs=[-0.75, 0.125]),
+                0: dict(f=(-1.0, 1.0), roc2=(0.05, 0.15),
+                        coefs=[-8.541667, 1.6, -0.2, 0.025396826, -0.0017857143])}
+
+
+def run_batched(args, rank, world, local):
+    """Batched workload: 64 uneven grids, FP32 fields (mixed), nt=100, one
+    persistent launch per fused pass vs looping the single-grid kernels."""
+    import torch
+    from girih_gb300 import gpu
+    torch.cuda.set_device(local)
+    nt = args.nt or 100
+    grids = batched_grids()
+    lups = sum(float(nx) * ny * nz for _, nx, ny, nz in grids) * 2 * ((nt + 1) // 2)
+    with gpu.Batch(grids, precision="mixed", device=local) as b:
+        for k, (op, nx, ny, nz) in enumerate(grids):
+            w = BATCH_INPUTS[op]
+            b.grid(k).fill_seeded(4000 + k, w["f"], w["roc2"], coefs=w["coefs"], f32_exact=True)
+        b.autotune()
+        res = {}
+        sampler = ClockSampler(local)
+        with sampler:
+            for name, fn in (("batched", b.run), ("looped", b.run_looped)):
+                for _ in range(args.warmup):
+                    fn(nt)
+                torch.cuda.synchronize()
+                ms = [fn(nt) for _ in range(args.steps)]
+                info = b.info()
+                res[name] = dict(glups=args.steps * lups / (sum(ms) / 1e3) / 1e9, ms_per_step=sum(ms) / args.steps,
+                                 launches_per_step=info["launches_last_run"], items_per_step=info["items_last_run"])
+        depths = b.info()["depths"]
+        # every grid against an FP64 plain run of its own, from the same inputs:
+        # re-seed the whole batch, one batched run of nt steps, then compare
+        for k, (op, nx, ny, nz) in enumerate(grids):
+            w = BATCH_INPUTS[op]
+            b.grid(k).fill_seeded(4000 + k, w["f"], w["roc2"], coefs=w["coefs"], f32_exact=True)
+        b.run(nt)
+        worst = {"max_rel": 0.0, "l2_rel": 0.0}
+        for k, (op, nx, ny, nz) in enumerate(grids):
+            w = BATCH_INPUTS[op]
+            with gpu.Context(op, nx, ny, nz, precision="fp64", schedule="plain", device=local) as ref:
+                ref.fill_seeded(4000 + k, w["f"], w["roc2"], coefs=w["coefs"], f32_exact=True)
+                ref.run(nt)
+                mr, l2 = gpu.rel_errors(b.grid(k).compare(ref))
+            worst["max_rel"] = max(worst["max_rel"], mr)
+            worst["l2_rel"] = max(worst["l2_rel"], l2)
+    return {"metric": "GLUP/s, 64 batched grids (7-pt and 25-pt leapfrog, FP32 fields), nt=100",
+            "value": res["batched"]["glups"], "unit": "GLUP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": res["batched"]["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, FP32-representable)",
+            "config": {"workload": "batched64", "grids": len(grids), "nt": nt,
+                       "points": sum(nx * ny * nz for _, nx, ny, nz in grids), "depths": depths},
+            "forms": res, "speedup_vs_looped": res["batched"]["glups"] / res["looped"]["glups"],
+            "errors": {"worst_grid": worst, "against": "FP64 plain run of each grid (single-grid path)"},
+            "clocks": sampler.summary(), "gpu_launches": args.steps * res["batched"]["launches_per_step"]}
+
+
 def cpu_baseline(wl, seconds, steps=None):
     """The oracle restatement (OpenMP over all host threads) on a bounded sample of
     the workload: the full grid, a few sweeps.  Returns the cpu_baseline object."""
@@ -336,7 +410,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="star7_leapfrog_512", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="star7_leapfrog_512", choices=sorted(WORKLOADS) + ["batched64"])
     ap.add_argument("--forms", default="")
     ap.add_argument("--headline", default="mixed")
     ap.add_argument("--depth", type=int, default=0)
@@ -348,6 +422,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     WORKLOAD_NAME = args.workload
+    if args.workload == "batched64":
+        rank, world, local = rank_env()
+        line = run_batched(args, rank, world, local)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        return
     wl = dict(WORKLOADS[args.workload])
     if args.n:
         wl["n"] = args.n

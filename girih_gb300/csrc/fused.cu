@@ -6,7 +6,8 @@ namespace girih {
 
 bool fused_supported(const Geom &g, int precision) {
   (void)precision;
-  return g.op == 0 || g.op == 1 || g.op == 8;
+  // the fused kernels index with 32-bit element offsets
+  return (g.op == 0 || g.op == 1 || g.op == 8) && g.elems < ((int64_t)1 << 31);
 }
 
 int fused_max_depth(const Geom &g, int precision) {

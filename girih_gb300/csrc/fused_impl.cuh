@@ -138,7 +138,9 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<T> &a, int bxi, int b
   T *sm = reinterpret_cast<T *>(smraw);
 
   const Geom &g = a.g;
-  const int64_t plane = g.plane;
+  // 32-bit element offsets: fused_supported() limits the fused schedule to
+  // grids of fewer than 2^31 elements per array
+  const int plane = (int)g.plane;
   const int X0 = bxi * BX, Y0 = byi * BY;
   const int Z0 = R + bzi * a.zchunk;
   const int Z1 = min(Z0 + a.zchunk, g.nnz - R);
@@ -165,7 +167,7 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<T> &a, int bxi, int b
   const bool xg_dom = x_dom[0] && x_dom[VX - 1];
 
   bool y_dom[CY], y_outr[CY];
-  int64_t col[CY];
+  int col[CY];
   unsigned act = 0;  // bit ((l-1)*CY + c)*VX + v
 #pragma unroll
   for (int c = 0; c < CY; c++) {
@@ -173,7 +175,7 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<T> &a, int bxi, int b
     y_dom[c] = yj + R >= 0 && yj + R < g.nny;
     const bool y_int = yj >= 0 && yj < g.ny;
     y_outr[c] = y_int && yj >= Y0 && yj < Y0 + BY;
-    col[c] = (int64_t)(yj + R) * g.px + g.ox + (xi0 + R);
+    col[c] = (yj + R) * g.px + g.ox + (xi0 + R);
 #pragma unroll
     for (int l = 1; l <= TT; l++)
       if (y_int && yj >= Y0 - (TT - l) * R && yj < Y0 + BY + (TT - l) * R)
@@ -206,7 +208,7 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<T> &a, int bxi, int b
       constexpr int RB = (PH + 1) & 1, WB = PH & 1;  // read buffer (s-1) and write buffer (s)
       const int s = sbase + PH;
       if (s > se) return;  // uniform over the CTA
-      const int64_t soff = (int64_t)s * plane;
+      const int soff = s * plane;
 
       // roc2 (and, for level 1, the old state) of every level, issued before the
       // level loop so that their latency overlaps the higher levels' arithmetic
@@ -218,7 +220,7 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<T> &a, int bxi, int b
           const bool p_int = p >= R && p < g.nnz - R;
 #pragma unroll
           for (int c = 0; c < CY; c++) {
-            const int64_t at = (int64_t)p * plane + col[c];
+            const int at = p * plane + col[c];
 #pragma unroll
             for (int v = 0; v < VX; v++) r2c[l - 1][c].e[v] = T(0);
             if (l == 1)
@@ -240,7 +242,7 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<T> &a, int bxi, int b
         const int p = s - L * D;
         const bool p_int = p >= R && p < g.nnz - R;
         const bool p_out = p_int && p >= Z0 && p < Z1;
-        const int64_t poff = soff - (int64_t)(L * D) * plane;
+        const int poff = soff - L * D * plane;
 #pragma unroll
         for (int c = 0; c < CY; c++) {
           const T *srow = thr + ((RB * TT + (L - 1)) * PR + c * NTY) * PW;

@@ -8,7 +8,8 @@ hot path: the whole nt=500 time loop over the 512^3 grid.
 
 Forms measured on the same grid, each from device-resident inputs:
   plain64  FP64, one sweep per kernel launch (the drop-in form)
-  fused64  FP64, time-fused passes
+  fused64  FP64, time-fused passes, FP64 arithmetic (bound by GB300's FP64 pipe)
+  fused64df FP64 fields, time-fused passes, double-float arithmetic (FP32 pairs)
   mixed    FP32 fields, compensated leapfrog, time-fused passes
 `value` is the headline form's GLUP/s (--headline, default mixed); `e2e` is the
 same form through the C ABI from pinned HOST arrays (upload + run + download).
@@ -141,6 +142,7 @@ def run_ours(args, wl, rank, world, local):
     forms = {
         "plain64": dict(precision="fp64", schedule="plain"),
         "fused64": dict(precision="fp64", schedule="fused"),
+        "fused64df": dict(precision="fp64df", schedule="fused"),
         "mixed": dict(precision="mixed", schedule="fused"),
     }
     if args.forms:
@@ -180,7 +182,7 @@ def run_ours(args, wl, rank, world, local):
             results[name] = dict(glups=world * args.steps * lups / dev_s / 1e9, ms_per_step=1e3 * dev_s / args.steps,
                                  wall_s=wall, launches_per_step=info["launches_last_run"],
                                  depth=info["fusion_depth"], tile=[info["block_x"], info["block_y"]],
-                                 kernel=info["kernel_name"], tsz=8 if kw["precision"] == "fp64" else 4,
+                                 kernel=info["kernel_name"], tsz=8 if kw["precision"] in ("fp64", "fp64df") else 4,
                                  schedule=kw["schedule"], precision=kw["precision"])
             ctxs[name] = ctx
     clocks = sampler.summary()

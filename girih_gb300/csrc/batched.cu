@@ -217,7 +217,7 @@ void fill_args(BatchGridArgs<T> &ga, const girih_gpu_ctx *c, int prev, int cur, 
   ga.a.roc2 = static_cast<const T *>(c->roc2);
   ga.a.out_prev = static_cast<T *>(c->f[oprev]);
   ga.a.out_cur = static_cast<T *>(c->f[ocur]);
-  for (int m = 0; m < 5; m++) ga.a.cc[m] = (T)c->cc[m];
+  for (int m = 0; m < 5; m++) ga.a.cc[m] = c->cc[m];
   ga.a.zchunk = zchunk;
   ga.a.write_prev = write_prev;
   ga.op = c->g.op;

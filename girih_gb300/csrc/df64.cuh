@@ -1,0 +1,88 @@
+// Double-float ("df64") arithmetic: a value is an unevaluated sum hi + lo of two
+// FP32 numbers, ~48 significant bits.  GB300 issues FP32 at 64x its FP64 rate,
+// so the fused kernels can keep FP64 data in HBM and do their arithmetic on
+// FP32 pairs.
+//
+// Algorithms (published, restated here): Knuth's TwoSum and Dekker's
+// FastTwoSum for error-free addition, and the FMA-based exact product
+// (Ogita, Rump, Oishi, "Accurate sum and dot product", 2005, Alg. 3.1/3.5 and
+// the TwoProduct-by-FMA variant).  Addition is the "sloppy" double-float sum
+// (one TwoSum of the high parts, the low parts added in FP32, renormalised),
+// whose absolute error is ~2^-48 (|a| + |b|).
+#pragma once
+#include <cstdint>
+
+namespace girih {
+
+struct Df64 {
+  float hi, lo;
+  Df64() = default;
+  __host__ __device__ constexpr Df64(float h, float l) : hi(h), lo(l) {}
+  __host__ __device__ constexpr Df64(int v) : hi((float)v), lo(0.f) {}
+  __host__ __device__ constexpr Df64(float v) : hi(v), lo(0.f) {}
+};
+
+__device__ __forceinline__ void df_fast_two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  e = __fsub_rn(b, __fsub_rn(s, a));
+}
+
+__device__ __forceinline__ void df_two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ Df64 operator+(Df64 a, Df64 b) {
+  float s, e;
+  df_two_sum(a.hi, b.hi, s, e);
+  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  Df64 r;
+  df_fast_two_sum(s, e, r.hi, r.lo);
+  return r;
+}
+
+__device__ __forceinline__ Df64 operator-(Df64 a) { return Df64(-a.hi, -a.lo); }
+__device__ __forceinline__ Df64 operator-(Df64 a, Df64 b) { return a + (-b); }
+
+__device__ __forceinline__ Df64 operator*(Df64 a, Df64 b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);  // exact error of the product
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  Df64 r;
+  df_fast_two_sum(p, e, r.hi, r.lo);
+  return r;
+}
+
+// Host-side split of a double constant into (hi, lo) with round-to-nearest hi.
+inline Df64 df_from_double_host(double d) {
+  const float h = (float)d;
+  return Df64(h, (float)(d - (double)h));
+}
+
+// Device split of an FP64 value using integer operations only (the FP64 pipe
+// is the scarce unit): hi = the top 24 significand bits (truncated), lo = the
+// next 29 bits rounded to 24.  Values outside the FP32 exponent range set
+// *range_bad and return 0; zeros and FP64 subnormals become 0.
+__device__ __forceinline__ Df64 df_split(double d, unsigned &range_bad) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const int E = (int)((b >> 52) & 0x7FF);
+  const int e = E - 1023;
+  if (E == 0 || e < -126) return Df64(0.f, 0.f);
+  if (e > 127) {
+    range_bad = 1u;
+    return Df64(0.f, 0.f);
+  }
+  const unsigned long long M = b & 0xFFFFFFFFFFFFFull;
+  const float hi = __uint_as_float(sign | ((unsigned)(e + 127) << 23) | (unsigned)(M >> 29));
+  const unsigned rem = (unsigned)(M & 0x1FFFFFFFull);  // value rem * 2^(e-52)
+  float lo = ldexpf(__uint2float_rn(rem), e - 52);
+  if (sign) lo = -lo;
+  return Df64(hi, lo);
+}
+
+__device__ __forceinline__ double df_to_double(Df64 x) { return (double)x.hi + (double)x.lo; }
+
+}  // namespace girih

@@ -1,5 +1,6 @@
 // Fused-schedule dispatch: which operators have a time-fused kernel, the tile
 // and depth for a grid, and the launch routed to the per-operator instantiations.
+#include "df64.cuh"
 #include "fused.cuh"
 
 namespace girih {
@@ -12,6 +13,7 @@ bool fused_supported(const Geom &g, int precision) {
 
 int fused_max_depth(const Geom &g, int precision) {
   if (g.r == 4) return 2;
+  if (precision == GIRIH_FP64_DF) return 3;
   return precision == GIRIH_FP64 ? 2 : 4;
 }
 
@@ -34,7 +36,7 @@ FusedConfig make_fused_config(const Geom &g, int precision, int depth, int varia
   int ntx, ry, vx;
   variant_shape(variant, g.r, &ntx, &ry, &vx);
   // double-buffered shared memory of all levels (rows padded by r) must fit one CTA (227 KiB)
-  const size_t tsz = precision == GIRIH_FP64 ? 8 : 4;
+  const size_t tsz = (precision == GIRIH_FP64 || precision == GIRIH_FP64_DF) ? 8 : 4;
   const int rp = (g.r + vx - 1) / vx * vx;
   if ((size_t)2 * depth * (ntx + 2 * rp) * (ry + 2 * g.r) * tsz > (size_t)227 * 1024) return c;
   c.depth = depth;
@@ -61,6 +63,14 @@ FusedConfig choose_fused_config(const Geom &g, int precision, int depth, int bx,
 cudaError_t launch_fused(const Geom &g, int tsz, int precision, const FusedConfig &cfg,
                          const FusedLaunch &L, cudaStream_t s) {
   const bool comp = precision == GIRIH_MIXED && g.to == 2;
+  if (precision == GIRIH_FP64_DF) {
+    switch (g.op) {
+      case 1: return launch_fused_op<1, Df64, false>(g, cfg, L, s);
+      case 8: return launch_fused_op<8, Df64, false>(g, cfg, L, s);
+      case 0: return launch_fused_op<0, Df64, false>(g, cfg, L, s);
+    }
+    return cudaErrorInvalidValue;
+  }
   switch (g.op) {
     case 1:
       return tsz == 8 ? launch_fused_op<1, double, false>(g, cfg, L, s)

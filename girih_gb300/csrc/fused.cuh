@@ -22,6 +22,7 @@ struct FusedLaunch {
   int steps;               // <= config depth
   int write_prev;          // time order 1: write state t+steps-1 (last pass only)
   double cc[5];
+  unsigned *range_flag;    // double-float compute: set if a value leaves the FP32 exponent range
 };
 
 bool fused_supported(const Geom &g, int precision);
@@ -47,6 +48,10 @@ GIRIH_FUSED_SPEC(8, float, true)
 GIRIH_FUSED_SPEC(0, double, false)
 GIRIH_FUSED_SPEC(0, float, false)
 GIRIH_FUSED_SPEC(0, float, true)
+struct Df64;
+GIRIH_FUSED_SPEC(1, Df64, false)
+GIRIH_FUSED_SPEC(8, Df64, false)
+GIRIH_FUSED_SPEC(0, Df64, false)
 #undef GIRIH_FUSED_SPEC
 
 }  // namespace girih

@@ -19,50 +19,95 @@
 // level below.
 #pragma once
 #include <algorithm>
+#include <type_traits>
 #include <utility>
 
+#include "df64.cuh"
 #include "fused.cuh"
 #include "ops.cuh"
 
 namespace girih {
 
-template <class T> struct FusedArgs {
+// Arguments of one fused pass over one grid.  S is the storage type in HBM
+// (float or double); the kernel computes in T (S itself, or Df64 for FP64
+// storage).
+template <class S> struct FusedArgs {
   Geom g;
-  const T *prev, *cur, *roc2;
-  T *out_prev, *out_cur;
-  T cc[5];
+  const S *prev, *cur, *roc2;
+  S *out_prev, *out_cur;
+  double cc[5];
   int zchunk;
   int write_prev;
+  unsigned *range_flag;  // Df64 compute: set when a value leaves the FP32 exponent range
 };
+
+// Storage type of a compute type.
+template <class T> struct StorageOf { using type = T; };
+template <> struct StorageOf<Df64> { using type = double; };
+
+// Conversions between storage and compute values.
+template <class T, class S> __device__ __forceinline__ T to_compute(S v, unsigned &bad) {
+  if constexpr (std::is_same<T, Df64>::value) return df_split(v, bad);
+  else return (T)v;
+}
+template <class S, class T> __device__ __forceinline__ S to_storage(T v) {
+  if constexpr (std::is_same<T, Df64>::value) return df_to_double(v);
+  else return (S)v;
+}
+template <class T> __device__ __forceinline__ T coef_to_compute(double c) {
+  if constexpr (std::is_same<T, Df64>::value) {
+    const float h = __double2float_rn(c);
+    return Df64(h, __double2float_rn(c - (double)h));
+  } else {
+    return (T)c;
+  }
+}
 
 // z-queue slot of plane p: planes are stored at p mod QL, so advancing a step
 // renames registers instead of moving them (the step loop is unrolled QL times
 // and every slot index below is a compile-time constant).
 template <int QL> __host__ __device__ constexpr int qslot(int x) { return ((x % QL) + QL) % QL; }
 
-// Vector of VX consecutive x elements (one thread owns VX columns).
-template <class T, int VX> struct VecT;
-template <> struct VecT<float, 1> { using type = float; };
-template <> struct VecT<float, 2> { using type = float2; };
-template <> struct VecT<double, 1> { using type = double; };
-template <> struct VecT<double, 2> { using type = double2; };
+// One aligned vector move of N bytes (4, 8 or 16).
+template <int N> struct VecBits;
+template <> struct VecBits<4> { using type = unsigned; };
+template <> struct VecBits<8> { using type = uint2; };
+template <> struct VecBits<16> { using type = uint4; };
 
+template <class X, int VX> union VecU {
+  typename VecBits<(int)sizeof(X) * VX>::type v;
+  X e[VX];
+  __device__ __forceinline__ VecU() {}
+};
+
+// VX consecutive x elements (one thread owns VX columns) in the compute type.
 template <class T, int VX> struct Pack {
   T e[VX];
+  // shared memory (compute type)
   __device__ __forceinline__ void load(const T *p) {
-    using V = typename VecT<T, VX>::type;
-    if constexpr (VX == 1) e[0] = p[0];
-    else { V v = *reinterpret_cast<const V *>(p); e[0] = v.x; e[1] = v.y; }
-  }
-  __device__ __forceinline__ void ldg(const T *p) {
-    using V = typename VecT<T, VX>::type;
-    if constexpr (VX == 1) e[0] = __ldg(p);
-    else { V v = __ldg(reinterpret_cast<const V *>(p)); e[0] = v.x; e[1] = v.y; }
+    VecU<T, VX> u;
+    u.v = *reinterpret_cast<const decltype(u.v) *>(p);
+#pragma unroll
+    for (int k = 0; k < VX; k++) e[k] = u.e[k];
   }
   __device__ __forceinline__ void store(T *p) const {
-    using V = typename VecT<T, VX>::type;
-    if constexpr (VX == 1) p[0] = e[0];
-    else { V v; v.x = e[0]; v.y = e[1]; *reinterpret_cast<V *>(p) = v; }
+    VecU<T, VX> u;
+#pragma unroll
+    for (int k = 0; k < VX; k++) u.e[k] = e[k];
+    *reinterpret_cast<decltype(u.v) *>(p) = u.v;
+  }
+  // global memory (storage type S), read-only path
+  template <class S> __device__ __forceinline__ void ldg(const S *p, unsigned &bad) {
+    VecU<S, VX> u;
+    u.v = __ldg(reinterpret_cast<const decltype(u.v) *>(p));
+#pragma unroll
+    for (int k = 0; k < VX; k++) e[k] = to_compute<T>(u.e[k], bad);
+  }
+  template <class S> __device__ __forceinline__ void stg(S *p) const {
+    VecU<S, VX> u;
+#pragma unroll
+    for (int k = 0; k < VX; k++) u.e[k] = to_storage<S>(e[k]);
+    *reinterpret_cast<decltype(u.v) *>(p) = u.v;
   }
 };
 
@@ -124,11 +169,14 @@ struct FusedShape {
 // executed by the NTX*NTY threads of the calling CTA (thread (tx, ty)).  Used by
 // the single-grid kernel below and by the batched persistent kernel.
 template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX>
-__device__ __forceinline__ void fused_tile(const FusedArgs<T> &a, int bxi, int byi, int bzi, int tx, int ty,
-                                           unsigned char *smraw) {
-  using S = FusedShape<OP, T, COMP, TT, NTX, NTY, CY, VX>;
-  constexpr int R = S::R, TO = S::TO, D = S::D, QL = S::QL, U = S::U;
-  constexpr int RW = S::RW, RY = S::RY, RP = S::RP, PW = S::PW, PR = S::PR, H = S::H, BX = S::BX, BY = S::BY;
+__device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>::type> &a, int bxi, int byi,
+                                           int bzi, int tx, int ty, unsigned char *smraw) {
+  using Sh = FusedShape<OP, T, COMP, TT, NTX, NTY, CY, VX>;
+  using ST = typename StorageOf<T>::type;
+  constexpr int R = Sh::R, TO = Sh::TO, D = Sh::D, QL = Sh::QL, U = Sh::U;
+  constexpr int RW = Sh::RW, RY = Sh::RY, RP = Sh::RP, PW = Sh::PW, PR = Sh::PR, H = Sh::H, BX = Sh::BX,
+                BY = Sh::BY;
+  unsigned range_bad = 0;
   static_assert(PW % VX == 0 && RP % VX == 0, "x groups must stay vector-aligned in shared memory");
   static_assert(BX > 0 && BY > 0, "tile too small for the fusion depth");
   static_assert(TT * CY * VX <= 32, "activity mask holds 32 (level, row, column) bits");
@@ -186,7 +234,7 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<T> &a, int bxi, int b
 
   T cc[5];
 #pragma unroll
-  for (int m = 0; m < 5; m++) cc[m] = a.cc[m];
+  for (int m = 0; m < 5; m++) cc[m] = coef_to_compute<T>(a.cc[m]);
 
   T q[TT][CY][VX][QL];
 #pragma unroll
@@ -227,8 +275,8 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<T> &a, int bxi, int b
 #pragma unroll
               for (int v = 0; v < VX; v++) pvc[c].e[v] = T(0);
             if (p_int && ((act >> (((l - 1) * CY + c) * VX)) & ((1u << VX) - 1))) {
-              r2c[l - 1][c].ldg(a.roc2 + at);
-              if (l == 1) pvc[c].ldg(a.prev + at);
+              r2c[l - 1][c].ldg(a.roc2 + at, range_bad);
+              if (l == 1) pvc[c].ldg(a.prev + at, range_bad);
             }
           }
         }
@@ -284,16 +332,16 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<T> &a, int bxi, int b
           });
           if constexpr (L == TT || L == TT - 1) {
             if (p_out && y_outr[c] && (L == TT || a.write_prev)) {
-              T *dst = (L == TT ? a.out_cur : a.out_prev) + poff + col[c];
+              ST *dst = (L == TT ? a.out_cur : a.out_prev) + poff + col[c];
               if (x_outc[0] && x_outc[VX - 1]) {
                 Pack<T, VX> o;
 #pragma unroll
                 for (int v = 0; v < VX; v++) o.e[v] = val[v];
-                o.store(dst);
+                o.stg(dst);
               } else {
 #pragma unroll
                 for (int v = 0; v < VX; v++)
-                  if (x_outc[v]) dst[v] = val[v];
+                  if (x_outc[v]) dst[v] = to_storage<ST>(val[v]);
               }
             }
           }
@@ -312,11 +360,11 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<T> &a, int bxi, int b
         for (int v = 0; v < VX; v++) in.e[v] = T(0);
         if (s_in && y_dom[c]) {
           if (xg_dom) {
-            in.ldg(a.cur + soff + col[c]);
+            in.ldg(a.cur + soff + col[c], range_bad);
           } else {
 #pragma unroll
             for (int v = 0; v < VX; v++)
-              if (x_dom[v]) in.e[v] = __ldg(a.cur + soff + col[c] + v);
+              if (x_dom[v]) in.e[v] = to_compute<T>(__ldg(a.cur + soff + col[c] + v), range_bad);
           }
         }
 #pragma unroll
@@ -325,7 +373,7 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<T> &a, int bxi, int b
           if (a.write_prev && s >= R && s < g.nnz - R && s >= Z0 && s < Z1 && y_outr[c])
 #pragma unroll
             for (int v = 0; v < VX; v++)
-              if (x_outc[v]) a.out_prev[soff + col[c] + v] = in.e[v];
+              if (x_outc[v]) a.out_prev[soff + col[c] + v] = to_storage<ST>(in.e[v]);
         }
       }
       // publish each level's centre plane (s - l*D - R) for the x/y neighbours of step s+1
@@ -341,10 +389,13 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<T> &a, int bxi, int b
       __syncthreads();
     });
   }
+  if constexpr (std::is_same<T, Df64>::value) {
+    if (range_bad && a.range_flag) atomicOr(a.range_flag, 1u);
+  }
 }
 
 template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX>
-__global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<T> a) {
+__global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<typename StorageOf<T>::type> a) {
   extern __shared__ __align__(16) unsigned char smraw[];
   fused_tile<OP, T, COMP, TT, NTX, NTY, CY, VX>(a, blockIdx.x, blockIdx.y, blockIdx.z, threadIdx.x, threadIdx.y,
                                                 smraw);
@@ -390,14 +441,16 @@ cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
   }
   const int zchunk = (g.nz + best_n - 1) / best_n;
   const int nz_ch = (g.nz + zchunk - 1) / zchunk;
-  FusedArgs<T> a{};
+  using ST = typename StorageOf<T>::type;
+  FusedArgs<ST> a{};
   a.g = g;
-  a.prev = static_cast<const T *>(L.prev);
-  a.cur = static_cast<const T *>(L.cur);
-  a.roc2 = static_cast<const T *>(L.roc2);
-  a.out_prev = static_cast<T *>(L.out_prev);
-  a.out_cur = static_cast<T *>(L.out_cur);
-  for (int m = 0; m < 5; m++) a.cc[m] = (T)L.cc[m];
+  a.prev = static_cast<const ST *>(L.prev);
+  a.cur = static_cast<const ST *>(L.cur);
+  a.roc2 = static_cast<const ST *>(L.roc2);
+  a.out_prev = static_cast<ST *>(L.out_prev);
+  a.out_cur = static_cast<ST *>(L.out_cur);
+  for (int m = 0; m < 5; m++) a.cc[m] = L.cc[m];
+  a.range_flag = L.range_flag;
   a.zchunk = zchunk;
   a.write_prev = L.write_prev;
   kern<<<dim3(gx, gy, nz_ch), dim3(NTX, NTY), smem, s>>>(a);
@@ -419,6 +472,7 @@ cudaError_t launch_variant(const Geom &g, const FusedLaunch &L, cudaStream_t s) 
 
 // Maximum fusion depth instantiated per operator radius and element type.
 template <int OP, class T> constexpr int fused_tmax() {
+  if constexpr (std::is_same<T, Df64>::value) return OpTraits<OP>::R == 4 ? 2 : 3;
   return OpTraits<OP>::R == 4 ? 2 : (sizeof(T) == 8 ? 2 : 4);
 }
 

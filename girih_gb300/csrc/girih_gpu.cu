@@ -279,6 +279,7 @@ int issue_steps_impl(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *
     L.steps = T;
     // time order 1 never reads state t-1, so only the last pass writes it (U1)
     L.write_prev = (c->g.to == 2 || left == T) ? 1 : 0;
+    L.range_flag = reinterpret_cast<unsigned *>(c->acc + 6);
     for (int m = 0; m < 5; m++) L.cc[m] = c->cc[m];
     cudaError_t e = launch_fused(c->g, c->tsz, c->d.precision, c->fcfg, L, st);
     if (e != cudaSuccess) return fail(GIRIH_GPU_ECUDA, std::string("fused launch: ") + cudaGetErrorString(e));
@@ -317,6 +318,7 @@ const char *girih_gpu_strerror(int err) {
     case GIRIH_GPU_ESTATE: return "call out of order";
     case GIRIH_GPU_ETIMEOUT: return "device-side wait timed out";
     case GIRIH_GPU_ENODEV: return "no usable CUDA device";
+    case GIRIH_GPU_ERANGE: return "value outside the range of the selected precision";
   }
   return "unknown error";
 }
@@ -335,7 +337,7 @@ int girih_gpu_create(girih_gpu_ctx **out, const girih_gpu_desc *d) {
   if (d->ldomain_shape[0] < nx + 2 * r || d->ldomain_shape[1] != ny + 2 * r || d->ldomain_shape[2] != nz + 2 * r)
     return fail(GIRIH_GPU_EINVAL, "ldomain_shape must be (>= nx+2r, ny+2r, nz+2r)");
   if (d->host_real_size != 4 && d->host_real_size != 8) return fail(GIRIH_GPU_EINVAL, "host_real_size must be 4 or 8");
-  if (d->precision < GIRIH_FP64 || d->precision > GIRIH_MIXED) return fail(GIRIH_GPU_EINVAL, "bad precision");
+  if (d->precision < GIRIH_FP64 || d->precision > GIRIH_FP64_DF) return fail(GIRIH_GPU_EINVAL, "bad precision");
   if (d->schedule < GIRIH_SCHED_PLAIN || d->schedule > GIRIH_SCHED_AUTO) return fail(GIRIH_GPU_EINVAL, "bad schedule");
   if ((int64_t)d->ldomain_shape[0] * d->ldomain_shape[1] > (int64_t)1 << 31)
     return fail(GIRIH_GPU_EINVAL, "x-y plane too large");
@@ -350,7 +352,7 @@ int girih_gpu_create(girih_gpu_ctx **out, const girih_gpu_desc *d) {
   girih_gpu_ctx *c = new (std::nothrow) girih_gpu_ctx;
   if (!c) return fail(GIRIH_GPU_ENOMEM, "host allocation failed");
   c->d = *d;
-  c->tsz = d->precision == GIRIH_FP64 ? 8 : 4;
+  c->tsz = (d->precision == GIRIH_FP64 || d->precision == GIRIH_FP64_DF) ? 8 : 4;
   c->hsz = d->host_real_size;
   c->bf16coef = d->precision == GIRIH_MIXED && var;
   c->g = make_geom(d->target_kernel, nx, ny, nz, d->ldomain_shape[0], c->tsz);
@@ -551,6 +553,9 @@ int girih_gpu_run(girih_gpu_ctx *c, int nt, float *ms_out) {
     c->g_new_iu1 = a;
     c->g_new_iu2 = b;
   }
+  const bool df = c->d.precision == GIRIH_FP64_DF && c->sched == GIRIH_SCHED_FUSED;
+  unsigned *range_flag = reinterpret_cast<unsigned *>(c->acc + 6);
+  if (df) CK(cudaMemsetAsync(range_flag, 0, sizeof(unsigned), c->st));
   CK(cudaEventRecord(c->e0, c->st));
   if (steps > 0) CK(cudaGraphLaunch(c->gexec, c->st));
   CK(cudaEventRecord(c->e1, c->st));
@@ -559,6 +564,16 @@ int girih_gpu_run(girih_gpu_ctx *c, int nt, float *ms_out) {
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, c->e0, c->e1));
   if (ms_out) *ms_out = ms;
+  if (df) {
+    unsigned bad = 0;
+    CK(cudaMemcpy(&bad, range_flag, sizeof(bad), cudaMemcpyDeviceToHost));
+    if (bad) {
+      c->iu1 = c->g_new_iu1;
+      c->iu2 = c->g_new_iu2;
+      return fail(GIRIH_GPU_ERANGE, "a field value left the FP32 exponent range of the double-float fused kernel; "
+                                    "use GIRIH_FP64 for this grid");
+    }
+  }
   c->iu1 = c->g_new_iu1;
   c->iu2 = c->g_new_iu2;
   c->last_launches = steps > 0 ? c->g_launches : 0;

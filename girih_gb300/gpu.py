@@ -17,16 +17,17 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libgirih_gpu.so")
 
-FP64, FP32, MIXED = 0, 1, 2
+FP64, FP32, MIXED, FP64_DF = 0, 1, 2, 3
 PLAIN, FUSED, AUTO = 0, 1, 2
-PRECISIONS = {"fp64": FP64, "fp32": FP32, "mixed": MIXED}
+PRECISIONS = {"fp64": FP64, "fp32": FP32, "mixed": MIXED, "fp64df": FP64_DF}
 SCHEDULES = {"plain": PLAIN, "fused": FUSED, "auto": AUTO}
 
 # radius, time order, number of coefficients, coefficient arrays?  (stencils.c:260-271; 8 is new)
 OP_INFO = {0: (4, 2, 5, False), 1: (1, 1, 2, False), 2: (1, 1, 2, True), 3: (1, 1, 4, True),
            4: (4, 1, 13, True), 5: (1, 1, 7, True), 8: (1, 2, 2, False)}
 
-ERRORS = {1: "EINVAL", 2: "EUNSUPPORTED", 3: "ECUDA", 4: "ENOMEM", 5: "ESTATE", 6: "ETIMEOUT", 7: "ENODEV"}
+ERRORS = {1: "EINVAL", 2: "EUNSUPPORTED", 3: "ECUDA", 4: "ENOMEM", 5: "ESTATE", 6: "ETIMEOUT", 7: "ENODEV",
+          8: "ERANGE"}
 
 
 class Desc(ctypes.Structure):

@@ -48,7 +48,8 @@ enum {
   GIRIH_GPU_ENOMEM = 4,       /* device allocation failed */
   GIRIH_GPU_ESTATE = 5,       /* call out of order (e.g. run before upload) */
   GIRIH_GPU_ETIMEOUT = 6,     /* a bounded device-side wait gave up */
-  GIRIH_GPU_ENODEV = 7        /* no usable CUDA device */
+  GIRIH_GPU_ENODEV = 7,       /* no usable CUDA device */
+  GIRIH_GPU_ERANGE = 8        /* a value left the range the selected precision can carry */
 };
 
 enum { GIRIH_OP_STAR7_LEAPFROG = 8 };
@@ -56,8 +57,12 @@ enum { GIRIH_OP_STAR7_LEAPFROG = 8 };
 enum {
   GIRIH_FP64 = 0,  /* FP64 fields and coefficients, FP64 arithmetic */
   GIRIH_FP32 = 1,  /* FP32 fields and coefficients, FP32 arithmetic */
-  GIRIH_MIXED = 2  /* FP32 fields; variable coefficients in BF16 with a per-array
+  GIRIH_MIXED = 2,  /* FP32 fields; variable coefficients in BF16 with a per-array
                       FP32 scale; FP32 accumulation; compensated leapfrog update */
+  GIRIH_FP64_DF = 3 /* FP64 fields in HBM; the fused schedule computes in double-float
+                      (pairs of FP32, ~48-bit significand; GB300 runs FP32 at 64x its FP64
+                      rate); run() returns GIRIH_GPU_ERANGE if a value leaves the FP32
+                      exponent range.  The plain schedule is the FP64 kernel. */
 };
 
 enum {

@@ -151,3 +151,41 @@ def test_autotune_restores_state_and_stays_correct(op, precision, sched):
     with gpu.Context(op, *_shape(op), precision=precision, schedule=sched) as ctx2:
         i2 = ctx2.info()
         assert (i2["schedule"], i2["fusion_depth"]) == (chosen["schedule"], chosen["fusion_depth"])
+
+
+@pytest.mark.parametrize("op", FUSED_OPS)
+@pytest.mark.parametrize("variant", [0, 1])
+def test_fused_double_float_within_fp64_bound(op, variant):
+    """FP64 storage, double-float arithmetic: held to the FP64 parity bound."""
+    r = gpu.OP_INFO[op][0]
+    g0 = oracle_grid(op, *_shape(op), seed=17)
+    nt = 9
+    ref = g0.copy().run(nt, nthreads=4)
+    for depth in range(1, (3 if r == 1 else 2) + 1):
+        with gpu_context(g0.copy(), precision="fp64df", schedule="fused", fusion_depth=depth,
+                         block=_block(op, depth, variant)) as ctx:
+            ctx.run(nt)
+            u1, u2 = ctx.download()
+        assert max_rel(u1, ref.U1, ref) <= FP64_TOL, (depth, max_rel(u1, ref.U1, ref))
+        assert max_rel(u2, ref.U2, ref) <= FP64_TOL, depth
+
+
+def test_fused_double_float_reference_init():
+    """The reference ramp + 100.1 boundary sources (operator 1, default coefficients)."""
+    g0 = oracle_grid(1, 45, 31, 27)
+    ref = g0.copy().run(20)
+    with gpu_context(g0.copy(), precision="fp64df", schedule="fused", fusion_depth=3) as ctx:
+        ctx.run(20)
+        u1, u2 = ctx.download()
+    assert max_rel(u1, ref.U1, ref) <= FP64_TOL
+    assert max_rel(u2, ref.U2, ref) <= FP64_TOL
+
+
+def test_fused_double_float_reports_range_overflow():
+    g = oracle_grid(1, 20, 20, 20, seed=1)
+    g.U1 *= 1e300
+    g.U2 *= 1e300
+    with gpu_context(g, precision="fp64df", schedule="fused") as ctx:
+        with pytest.raises(gpu.GirihGpuError) as e:
+            ctx.run(2)
+        assert e.value.code == 8

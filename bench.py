@@ -261,7 +261,8 @@ def run_ours(args, wl, rank, world, local):
         "metric": "GLUP/s at 512^3: time-fused & mixed vs plain FP64 on GB300; % HBM roofline; err",
         "value": h["glups"], "unit": "GLUP/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": h["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32" if h["precision"] != "fp64" else "f64", "data": "synthetic (seeded SplitMix64, FP32-representable)",
+        "dtype": {"fp64": "f64", "fp64df": "df64 (FP32 pairs)"}.get(h["precision"], "f32"),
+        "data": "synthetic (seeded SplitMix64, FP32-representable)",
         "config": {"workload": WORKLOAD_NAME, "operator": op, "grid": [n, n, n], "nt": nt, "headline_form": head,
                    "fusion_depth": h["depth"], "tile": h["tile"],
                    "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (no flush needed)"},

@@ -43,6 +43,7 @@ __device__ __forceinline__ Df64 operator+(Df64 a, Df64 b) {
 }
 
 __device__ __forceinline__ Df64 operator-(Df64 a) { return Df64(-a.hi, -a.lo); }
+__device__ __forceinline__ Df64 twice(Df64 a) { return Df64(2.f * a.hi, 2.f * a.lo); }  // exact
 __device__ __forceinline__ Df64 operator-(Df64 a, Df64 b) { return a + (-b); }
 
 __device__ __forceinline__ Df64 operator*(Df64 a, Df64 b) {

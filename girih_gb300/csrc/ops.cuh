@@ -29,6 +29,10 @@ struct FastArith {
   template <class T> static __device__ __forceinline__ T sub(T a, T b) { return a - b; }
 };
 
+// 2v, exactly: v + v for IEEE types (bit-identical to 2*v); a double-float
+// type supplies its own exact scaling by overloading twice().
+template <class T> __device__ __forceinline__ T twice(T v) { return v + v; }
+
 // Operator metadata (src/kernels/stencils.c:260-271, plus id 8).
 template <int OP> struct OpTraits;
 template <> struct OpTraits<0> { static constexpr int R = 4, TO = 2, NC = 5, VAR = 0; };
@@ -84,7 +88,7 @@ __device__ __forceinline__ T apply_op(const T *cc, const Cf &coef, int64_t cidx,
     constexpr int R = OpTraits<OP>::R;
     T lap = star_const_sum<R, A>(cc, V);
     // u = 2v - u + roc2*lap   (verification.c:344-348)
-    return A::add(A::sub(A::mul(T(2), V.c()), uold), A::mul(roc2, lap));
+    return A::add(A::sub(twice(V.c()), uold), A::mul(roc2, lap));
   } else if constexpr (OP == 1) {
     return star_const_sum<1, A>(cc, V);
   } else if constexpr (OP == 2) {  // verification.c:390-393

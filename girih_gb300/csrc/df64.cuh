@@ -79,7 +79,9 @@ __device__ __forceinline__ Df64 df_split(double d, unsigned &range_bad) {
   const unsigned long long M = b & 0xFFFFFFFFFFFFFull;
   const float hi = __uint_as_float(sign | ((unsigned)(e + 127) << 23) | (unsigned)(M >> 29));
   const unsigned rem = (unsigned)(M & 0x1FFFFFFFull);  // value rem * 2^(e-52)
-  float lo = ldexpf(__uint2float_rn(rem), e - 52);
+  // scale by 2^(e-52) through the exponent field; below 2^-74 the low part is
+  // under the FP32 normal range and is dropped (relative size < 2^-48 of hi)
+  float lo = e >= -74 ? __uint2float_rn(rem) * __uint_as_float((unsigned)(e - 52 + 127) << 23) : 0.f;
   if (sign) lo = -lo;
   return Df64(hi, lo);
 }

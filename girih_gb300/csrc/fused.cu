@@ -13,7 +13,7 @@ bool fused_supported(const Geom &g, int precision) {
 
 int fused_max_depth(const Geom &g, int precision) {
   if (g.r == 4) return 2;
-  if (precision == GIRIH_FP64_DF) return 2;
+  if (precision == GIRIH_FP64_DF) return 3;
   return precision == GIRIH_FP64 ? 2 : 4;
 }
 

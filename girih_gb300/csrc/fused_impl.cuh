@@ -479,7 +479,7 @@ cudaError_t launch_variant(const Geom &g, const FusedLaunch &L, cudaStream_t s) 
 
 // Maximum fusion depth instantiated per operator radius and element type.
 template <int OP, class T> constexpr int fused_tmax() {
-  if constexpr (std::is_same<T, Df64>::value) return 2;  // deeper double-float pipelines spill
+  if constexpr (std::is_same<T, Df64>::value) return OpTraits<OP>::R == 4 ? 2 : 3;
   return OpTraits<OP>::R == 4 ? 2 : (sizeof(T) == 8 ? 2 : 4);
 }
 

@@ -161,7 +161,7 @@ def test_fused_double_float_within_fp64_bound(op, variant):
     g0 = oracle_grid(op, *_shape(op), seed=17)
     nt = 9
     ref = g0.copy().run(nt, nthreads=4)
-    for depth in (1, 2):
+    for depth in range(1, (3 if r == 1 else 2) + 1):
         with gpu_context(g0.copy(), precision="fp64df", schedule="fused", fusion_depth=depth,
                          block=_block(op, depth, variant)) as ctx:
             ctx.run(nt)
@@ -174,7 +174,7 @@ def test_fused_double_float_reference_init():
     """The reference ramp + 100.1 boundary sources (operator 1, default coefficients)."""
     g0 = oracle_grid(1, 45, 31, 27)
     ref = g0.copy().run(20)
-    with gpu_context(g0.copy(), precision="fp64df", schedule="fused", fusion_depth=2) as ctx:
+    with gpu_context(g0.copy(), precision="fp64df", schedule="fused", fusion_depth=3) as ctx:
         ctx.run(20)
         u1, u2 = ctx.download()
     assert max_rel(u1, ref.U1, ref) <= FP64_TOL

@@ -32,6 +32,7 @@ int op_info(int op, int *r, int *to, int *nc, int *var) {
     case 3: R = 1; TO = 1; NC = 4; VAR = 1; break;
     case 4: R = 4; TO = 1; NC = 13; VAR = 1; break;
     case 5: R = 1; TO = 1; NC = 7; VAR = 1; break;
+    case 7: R = 1; TO = 1; NC = 4; VAR = 0; break;
     case 8: R = 1; TO = 2; NC = 2; VAR = 0; break;
     default: return -1;
   }
@@ -442,7 +443,7 @@ int girih_gpu_upload(girih_gpu_ctx *c, const void *U1, const void *U2, const voi
   if (g.to == 2 && (e = upload_field(c, U3, c->roc2))) return e;
   if (!g.var) {
     for (int m = 0; m < 5; m++)
-      c->cc[m] = m <= g.r ? (c->hsz == 8 ? static_cast<const double *>(coef)[m]
+      c->cc[m] = m < g.nc ? (c->hsz == 8 ? static_cast<const double *>(coef)[m]
                                          : (double)static_cast<const float *>(coef)[m])
                           : 0.0;
   } else {
@@ -509,7 +510,7 @@ int girih_gpu_fill_seeded(girih_gpu_ctx *c, uint64_t seed, const double ranges[6
       }
     }
   } else {
-    for (int m = 0; m < 5; m++) c->cc[m] = m <= g.r ? const_coefs[m] : 0.0;
+    for (int m = 0; m < 5; m++) c->cc[m] = m < g.nc ? const_coefs[m] : 0.0;
   }
   c->iu1 = 0;
   c->iu2 = 1;

@@ -41,6 +41,7 @@ template <> struct OpTraits<2> { static constexpr int R = 1, TO = 1, NC = 2, VAR
 template <> struct OpTraits<3> { static constexpr int R = 1, TO = 1, NC = 4, VAR = 1; };
 template <> struct OpTraits<4> { static constexpr int R = 4, TO = 1, NC = 13, VAR = 1; };
 template <> struct OpTraits<5> { static constexpr int R = 1, TO = 1, NC = 7, VAR = 1; };
+template <> struct OpTraits<7> { static constexpr int R = 1, TO = 1, NC = 4, VAR = 0; };
 template <> struct OpTraits<8> { static constexpr int R = 1, TO = 2, NC = 2, VAR = 0; };
 
 // Coefficient fetch for variable-coefficient operators: array m at the centre
@@ -121,6 +122,22 @@ __device__ __forceinline__ T apply_op(const T *cc, const Cf &coef, int64_t cidx,
     s = A::add(s, A::mul(T(coef(4, cidx)), V.y(1)));
     s = A::add(s, A::mul(T(coef(5, cidx)), V.z(-1)));
     s = A::add(s, A::mul(T(coef(6, cidx)), V.z(1)));
+    return s;
+  } else if constexpr (OP == 7) {  // box, verification.c:797-815: edges and corners via V.xyz()
+    T s = A::mul(cc[0], V.c());
+    s = A::add(s, A::mul(cc[1], GIRIH_PAIR(x, 1)));
+    s = A::add(s, A::mul(cc[1], GIRIH_PAIR(y, 1)));
+    s = A::add(s, A::mul(cc[1], GIRIH_PAIR(z, 1)));
+    s = A::add(s, A::mul(cc[2], A::add(V.xyz(1, 0, -1), V.xyz(-1, 0, -1))));
+    s = A::add(s, A::mul(cc[2], A::add(V.xyz(0, 1, -1), V.xyz(0, -1, -1))));
+    s = A::add(s, A::mul(cc[2], A::add(V.xyz(1, 1, 0), V.xyz(-1, -1, 0))));
+    s = A::add(s, A::mul(cc[2], A::add(V.xyz(1, -1, 0), V.xyz(-1, 1, 0))));
+    s = A::add(s, A::mul(cc[2], A::add(V.xyz(1, 0, 1), V.xyz(-1, 0, 1))));
+    s = A::add(s, A::mul(cc[2], A::add(V.xyz(0, 1, 1), V.xyz(0, -1, 1))));
+    s = A::add(s, A::mul(cc[3], A::add(V.xyz(1, 1, 1), V.xyz(-1, -1, -1))));
+    s = A::add(s, A::mul(cc[3], A::add(V.xyz(1, -1, 1), V.xyz(-1, 1, -1))));
+    s = A::add(s, A::mul(cc[3], A::add(V.xyz(-1, -1, 1), V.xyz(1, 1, -1))));
+    s = A::add(s, A::mul(cc[3], A::add(V.xyz(-1, 1, 1), V.xyz(1, -1, -1))));
     return s;
   }
   return T(0);

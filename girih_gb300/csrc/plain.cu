@@ -19,11 +19,14 @@ constexpr int kBX = 32, kBY = 8;
 template <int R, class T> struct ColumnAcc {
   const T *__restrict__ p;  // centre point in v
   int64_t sy;               // row pitch
+  int64_t sz;               // plane pitch
   const T (&q)[2 * R + 1];  // column values at planes k-R .. k+R
   __device__ __forceinline__ T c() const { return q[R]; }
   __device__ __forceinline__ T x(int d) const { return __ldg(p + d); }
   __device__ __forceinline__ T y(int d) const { return __ldg(p + d * sy); }
   __device__ __forceinline__ T z(int d) const { return q[R + d]; }
+  // off-axis neighbour (box operator)
+  __device__ __forceinline__ T xyz(int dx, int dy, int dz) const { return __ldg(p + dx + dy * sy + dz * sz); }
 };
 
 template <int OP, class A, class T, class Cf>
@@ -45,7 +48,7 @@ __global__ void __launch_bounds__(kBX *kBY) plain_step(StepArgs<T> a, Cf coef, i
   for (int d = 0; d < 2 * R; d++) q[d] = __ldg(a.v + c + (int64_t)(d - R) * plane);
   for (int k = k0; k < k1; k++, c += plane) {
     q[2 * R] = __ldg(a.v + c + (int64_t)R * plane);
-    ColumnAcc<R, T> acc{a.v + c, a.g.px, q};
+    ColumnAcc<R, T> acc{a.v + c, a.g.px, plane, q};
     T uold = T(0), r2 = T(0);
     if constexpr (TO == 2) {
       uold = a.u[c];
@@ -102,6 +105,7 @@ cudaError_t launch_plain(const StepArgs<T> &a, bool exact, bool bf16coef, cudaSt
     case 3: return dispatch<3>(a, exact, bf16coef, s);
     case 4: return dispatch<4>(a, exact, bf16coef, s);
     case 5: return dispatch<5>(a, exact, bf16coef, s);
+    case 7: return dispatch<7>(a, exact, bf16coef, s);
     case 8: return dispatch<8>(a, exact, bf16coef, s);
   }
   return cudaErrorInvalidValue;

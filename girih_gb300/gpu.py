@@ -24,7 +24,7 @@ SCHEDULES = {"plain": PLAIN, "fused": FUSED, "auto": AUTO}
 
 # radius, time order, number of coefficients, coefficient arrays?  (stencils.c:260-271; 8 is new)
 OP_INFO = {0: (4, 2, 5, False), 1: (1, 1, 2, False), 2: (1, 1, 2, True), 3: (1, 1, 4, True),
-           4: (4, 1, 13, True), 5: (1, 1, 7, True), 8: (1, 2, 2, False)}
+           4: (4, 1, 13, True), 5: (1, 1, 7, True), 7: (1, 1, 4, False), 8: (1, 2, 2, False)}
 
 ERRORS = {1: "EINVAL", 2: "EUNSUPPORTED", 3: "ECUDA", 4: "ENOMEM", 5: "ESTATE", 6: "ETIMEOUT", 7: "ENODEV",
           8: "ERANGE"}

@@ -27,6 +27,7 @@
  *   3  star r=1, variable axis-symmetric, 4  (..._var_axsym, :121-126)
  *   4  star r=4, variable axis-symmetric, 13 (iso_ref_8space_1time_var_axsym, :148-162)
  *   5  star r=1, variable no-symmetry, 7     (..._var_nosym, :193-201)
+ *   7  box 27-point, constant coef, 4 scalars (box_ref_2space_1time, :227-242; plain schedule)
  *   8  star r=1, time order 2, constant coef (radius-1 analogue of 0; no reference id)
  */
 #ifndef GIRIH_GPU_H

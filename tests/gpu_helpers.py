@@ -17,6 +17,7 @@ SEED_PARAMS = {  # op -> (f range, roc2 range, coef range, constant coefs)
     3: ((0.0, 1.0), (0.0, 0.0), (0.01, 0.1), None),
     4: ((0.0, 1.0), (0.0, 0.0), (0.01, 0.025), None),
     5: ((0.0, 1.0), (0.0, 0.0), (0.01, 0.1), None),
+    7: ((0.0, 1.0), (0.0, 0.0), (0.0, 0.0), [-0.5, 0.05, 0.02, 0.01]),  # box: 4 constant coefficients
     8: ((0.0, 1.0), (0.5, 1.5), (0.0, 0.0), LAP2),
 }
 

@@ -145,7 +145,7 @@ def test_float_host_arrays():
 
 def test_error_codes():
     with pytest.raises(gpu.GirihGpuError) as e:
-        gpu.Context(7, 8, 8, 8)  # box operator: not provided on the GPU
+        gpu.Context(6, 8, 8, 8)  # solar operator: not a star/box operator on the GPU
     assert e.value.code == 2
     with pytest.raises(gpu.GirihGpuError) as e:
         gpu.Context(1, 0, 8, 8)

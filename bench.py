@@ -100,6 +100,18 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(x, device=None):
+    """Max of a float over all ranks (the slowest rank sets the job time); the
+    identity without torch.distributed."""
+    import torch
+    import torch.distributed as tdist
+    if not (tdist.is_available() and tdist.is_initialized()) or tdist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def measured_peak_hbm():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -173,11 +185,7 @@ def run_ours(args, wl, rank, world, local):
                 ms.append(ctx.run(nt))
             barrier_sync()
             wall = time.perf_counter() - t0
-            dev_s = sum(ms) / 1e3
-            if dist:
-                t = torch.tensor([dev_s], dtype=torch.float64, device="cuda")
-                tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-                dev_s = float(t.item())
+            dev_s = max_over_ranks(sum(ms) / 1e3, "cuda")
             info = ctx.info()
             results[name] = dict(glups=world * args.steps * lups / dev_s / 1e9, ms_per_step=1e3 * dev_s / args.steps,
                                  wall_s=wall, launches_per_step=info["launches_last_run"],
@@ -244,11 +252,7 @@ def run_ours(args, wl, rank, world, local):
             ectx.run(nt)
             ectx.download(host[0].data_ptr(), None)
         barrier_sync()
-        wall = time.perf_counter() - t0
-        if dist:
-            t = torch.tensor([wall], dtype=torch.float64, device="cuda")
-            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-            wall = float(t.item())
+        wall = max_over_ranks(time.perf_counter() - t0, "cuda")
         nbytes = host[0].numel() * 8
         e2e = {"value": world * args.steps * lups / wall / 1e9, "unit": "GLUP/s",
                "h2d_bytes_per_step": nbytes * (3 if u3 else 2), "d2h_bytes_per_step": nbytes,
@@ -417,7 +421,8 @@ def main():
     ap.add_argument("--forms", default="")
     ap.add_argument("--headline", default="mixed")
     ap.add_argument("--depth", type=int, default=0)
-    ap.add_argument("--n", type=int, default=0, help="override the grid edge (small profiling cases)")
+    ap.add_argument("--grid", "--n", dest="n", type=int, default=0,
+                    help="override the grid edge (small profiling cases)")
     ap.add_argument("--nt", type=int, default=0, help="override the number of time steps")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-e2e", action="store_true")

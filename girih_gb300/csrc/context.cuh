@@ -1,6 +1,8 @@
 // Internal layout of a girih_gpu_ctx, shared by the single-grid entry points
 // (girih_gpu.cu) and the batched entry points (batched.cu).
 #pragma once
+#include <cuda.h>
+
 #include "fused.cuh"
 #include "internal.cuh"
 
@@ -29,6 +31,9 @@ struct girih_gpu_ctx {
   int g_launches = 0, g_new_iu1 = 0, g_new_iu2 = 1;
   int last_launches = 0, last_steps = 0;
   double dev_bytes = 0;
+  // TMA tensor maps of the four field buffers and roc2 (index 4), per TMA variant (2, 3)
+  CUtensorMap tmaps[5][2];
+  bool tmap_ok[5][2] = {{false, false}, {false, false}, {false, false}, {false, false}, {false, false}};
 };
 
 namespace girih {

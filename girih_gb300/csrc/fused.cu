@@ -21,10 +21,11 @@ int fused_max_depth(const Geom &g, int precision) {
 //   radius 1 (x pairs per thread): variant 0 = 64 x 32 (32x16 threads, 2 rows
 //   each), variant 1 = 32 x 64 (16x64 threads, 1 row each);
 //   radius 4 (one column per thread): variant 0 = 64 x 32 (64x16 threads, 2
-//   rows), variant 1 = 32 x 64 (32x32 threads, 2 rows).
+//   rows), variant 1 = 32 x 64 (32x32 threads, 2 rows);
+//   variants 2 and 3: 0 and 1 with TMA-staged input planes.
 static void variant_shape(int v, int r, int *ntx, int *ry, int *vx) {
-  *ntx = v == 0 ? 64 : 32;
-  *ry = v == 0 ? 32 : 64;
+  *ntx = (v % 2) == 0 ? 64 : 32;
+  *ry = (v % 2) == 0 ? 32 : 64;
   *vx = r == 1 ? 2 : 1;
 }
 
@@ -35,13 +36,26 @@ FusedConfig make_fused_config(const Geom &g, int precision, int depth, int varia
     return c;
   int ntx, ry, vx;
   variant_shape(variant, g.r, &ntx, &ry, &vx);
-  // double-buffered shared memory of all levels (rows padded by r) must fit one CTA (227 KiB)
+  // double-buffered shared memory of all levels (rows padded by r), plus the TMA
+  // rings of the TMA variants, must fit one CTA (227 KiB)
   const size_t tsz = (precision == GIRIH_FP64 || precision == GIRIH_FP64_DF) ? 8 : 4;
+  const bool tma = variant >= 2;
+  if (tma && tsz != 4) return c;  // TMA variants are built for FP32 storage
   const int rp = (g.r + vx - 1) / vx * vx;
-  if ((size_t)2 * depth * (ntx + 2 * rp) * (ry + 2 * g.r) * tsz > (size_t)227 * 1024) return c;
+  size_t smem = (size_t)2 * depth * (ntx + 2 * rp) * (ry + 2 * g.r) * tsz;
+  int align = vx;
+  if (tma) {
+    const int nb = fused_tma_nb(g.r, depth), nr = fused_tma_nr(g.r, depth, nb);
+    const size_t plane = (size_t)ntx * ry * tsz;
+    smem = (smem + 127) / 128 * 128 + nb * plane + (g.to == 2 ? (nb + nr) * plane : 0) + nb * 8;
+    align = 16 / (int)tsz > vx ? 16 / (int)tsz : vx;
+    c.box_w = ntx;
+    c.box_h = ry;
+  }
+  if (smem > (size_t)227 * 1024) return FusedConfig{};
   c.depth = depth;
   c.variant = variant;
-  c.bx = ntx - 2 * depth * g.r - (vx - 1);  // pairs lose one column to their alignment
+  c.bx = ntx - 2 * depth * g.r - (align - 1);  // the region start is aligned to `align` columns
   c.by = ry - 2 * depth * g.r;
   if (c.bx <= 0 || c.by <= 0) c.depth = 0;
   return c;

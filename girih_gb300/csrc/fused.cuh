@@ -5,14 +5,25 @@
 namespace girih {
 
 // Thread-block shapes of the fused kernel.  A CTA covers an input region of
-// NTX x (NTY*CY) columns (tile + halo of depth*R on every side); each thread
-// owns one x column and CY rows of it and streams the whole z range.
-enum FusedVariant { FV_64x32_512 = 0, FV_32x64_1024 = 1, FV_COUNT = 2 };
+// columns (tile + halo of depth*R on every side); each thread owns VX x columns
+// and CY rows of it and streams the whole z range.  Variants 2 and 3 are
+// variants 0 and 1 with the input planes staged into shared memory by TMA.
+enum FusedVariant { FV_64x32_512 = 0, FV_32x64_1024 = 1, FV_64x32_512_TMA = 2, FV_32x64_1024_TMA = 3, FV_COUNT = 4 };
+
+// TMA ring depths: NB planes of the input (and old) state in flight, NR planes
+// of roc2 (level l reads roc2 (l-1)*(R+1) planes after level 1 did).
+__host__ __device__ constexpr int fused_tma_nb(int r, int tt) { return (r == 4 || tt >= 4) ? 2 : 4; }
+__host__ __device__ constexpr int fused_tma_nr(int r, int tt, int nb) {
+  int need = (tt - 1) * (r + 1) + nb, p = 1;
+  while (p < need) p *= 2;
+  return p;
+}
 
 struct FusedConfig {
   int depth = 0;    // time steps per pass (0 = not available)
   int variant = 0;  // FusedVariant
   int bx = 0, by = 0;  // output tile of one CTA
+  int box_w = 0, box_h = 0;  // TMA box (region) of the variant, 0 without TMA
 };
 
 struct FusedLaunch {
@@ -22,7 +33,9 @@ struct FusedLaunch {
   int steps;               // <= config depth
   int write_prev;          // time order 1: write state t+steps-1 (last pass only)
   double cc[5];
-  unsigned *range_flag;    // double-float compute: set if a value leaves the FP32 exponent range
+  unsigned *range_flag;    // bit 0: a value left the FP32 exponent range (double-float);
+                           // bit 1: a TMA copy did not complete within the wait bound
+  const void *tma_cur, *tma_prev, *tma_roc2;  // host CUtensorMap objects (TMA variants)
 };
 
 bool fused_supported(const Geom &g, int precision);

@@ -25,6 +25,7 @@
 #include "df64.cuh"
 #include "fused.cuh"
 #include "ops.cuh"
+#include "tma.cuh"
 
 namespace girih {
 
@@ -150,8 +151,9 @@ __device__ __forceinline__ float leapfrog_compensated(float v, float u, float r2
 __device__ __forceinline__ int pmod(int a, int m) { return ((a % m) + m) % m; }
 
 
-template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX>
+template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX, bool TMA = false>
 struct FusedShape {
+  using ST = typename StorageOf<T>::type;
   static constexpr int R = OpTraits<OP>::R;
   static constexpr int TO = OpTraits<OP>::TO;
   static constexpr int D = R + 1;                            // planes between time levels
@@ -161,17 +163,29 @@ struct FusedShape {
   static constexpr int RP = (R + VX - 1) / VX * VX;           // column padding, a whole number of x groups
   static constexpr int PW = RW + 2 * RP, PR = RY + 2 * R;     // shared rows padded by RP, rows by R
   static constexpr int H = TT * R;
-  static constexpr int BX = RW - 2 * H - (VX - 1), BY = RY - 2 * H;  // output tile
-  static constexpr size_t smem_bytes = (size_t)2 * TT * PR * PW * sizeof(T);
+  // x alignment of the region start: one x group, or 16 bytes for TMA boxes
+  static constexpr int ALIGN = TMA ? (16 / (int)sizeof(ST) > VX ? 16 / (int)sizeof(ST) : VX) : VX;
+  static constexpr int BX = RW - 2 * H - (ALIGN - 1), BY = RY - 2 * H;  // output tile
+  static constexpr size_t field_bytes = (size_t)2 * TT * PR * PW * sizeof(T);
+  // TMA rings: NB planes of the input state (and the old state), NR planes of roc2
+  static constexpr int NB = fused_tma_nb(R, TT);
+  static constexpr int NR = fused_tma_nr(R, TT, NB);
+  static constexpr size_t plane_bytes = (size_t)RW * RY * sizeof(ST);
+  static constexpr size_t off_cur = (field_bytes + 127) / 128 * 128;
+  static constexpr size_t off_prev = off_cur + NB * plane_bytes;
+  static constexpr size_t off_roc2 = off_prev + (TO == 2 ? NB * plane_bytes : 0);
+  static constexpr size_t off_bar = off_roc2 + (TO == 2 ? NR * plane_bytes : 0);
+  static constexpr size_t smem_bytes = TMA ? off_bar + NB * sizeof(uint64_t) : field_bytes;
 };
 
 // One CTA-tile of a fused pass: tile (bxi, byi) of the x-y tiling, z chunk bzi,
 // executed by the NTX*NTY threads of the calling CTA (thread (tx, ty)).  Used by
 // the single-grid kernel below and by the batched persistent kernel.
-template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX>
+template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX, bool TMA = false>
 __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>::type> &a, int bxi, int byi,
-                                           int bzi, int tx, int ty, unsigned char *smraw) {
-  using Sh = FusedShape<OP, T, COMP, TT, NTX, NTY, CY, VX>;
+                                           int bzi, int tx, int ty, unsigned char *smraw,
+                                           const TmaMaps *maps = nullptr) {
+  using Sh = FusedShape<OP, T, COMP, TT, NTX, NTY, CY, VX, TMA>;
   using ST = typename StorageOf<T>::type;
   constexpr int R = Sh::R, TO = Sh::TO, D = Sh::D, QL = Sh::QL, U = Sh::U;
   constexpr int RW = Sh::RW, RY = Sh::RY, RP = Sh::RP, PW = Sh::PW, PR = Sh::PR, H = Sh::H, BX = Sh::BX,
@@ -196,8 +210,9 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
   const int se = Z1 - 1 + TT * D;
   const int s0 = sb - sb % U;  // plane p lives in queue slot p mod QL; buffer parity = PH parity
 
-  // region start, aligned so that every thread's x-group is one aligned vector in memory
-  const int xs = X0 - H - pmod(X0 - H + R + g.ox, VX);
+  // region start, aligned so that every thread's x-group is one aligned vector
+  // in memory (and, for TMA, so that the box starts on a 16-byte boundary)
+  const int xs = X0 - H - pmod(X0 - H + R + g.ox, Sh::ALIGN);
   const int xi0 = xs + tx * VX;  // interior x index of the thread's first column
 
   bool x_dom[VX], x_outc[VX];
@@ -250,6 +265,40 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
   //   sm + thr + ((b*TT + l)*PR + c*NTY)*PW   (compile-time offsets from thr)
   T *const thr = sm + (ty + R) * PW + tx * VX + RP;
 
+  // TMA: one thread streams whole region planes into shared-memory rings,
+  // NB-1 planes ahead of the z step that consumes them
+  constexpr int NB = Sh::NB, NR = Sh::NR;
+  const int tid = ty * NTX + tx;
+  ST *const ring_cur = reinterpret_cast<ST *>(smraw + Sh::off_cur);
+  ST *const ring_prev = reinterpret_cast<ST *>(smraw + Sh::off_prev);
+  ST *const ring_roc2 = reinterpret_cast<ST *>(smraw + Sh::off_roc2);
+  uint64_t *const bars = reinterpret_cast<uint64_t *>(smraw + Sh::off_bar);
+  const int xg = xs + R + g.ox, yg = Y0 - H + R;  // global x / row of the region origin
+  unsigned tma_timeout = 0;
+  auto tma_issue = [&](int t) {  // input planes of z step t (thread 0 only)
+    if constexpr (TMA) {
+      const int k = (t - s0) & (NB - 1);
+      unsigned bytes = (unsigned)Sh::plane_bytes;
+      if constexpr (TO == 2) bytes *= 3;
+      fence_proxy_async_smem();
+      mbar_arrive_expect_tx(&bars[k], bytes);
+      tma_load_3d(ring_cur + (size_t)k * RW * RY, &maps->cur, xg, yg, t, &bars[k]);
+      if constexpr (TO == 2) {
+        tma_load_3d(ring_prev + (size_t)k * RW * RY, &maps->prev, xg, yg, t - D, &bars[k]);
+        tma_load_3d(ring_roc2 + (size_t)((t - s0) & (NR - 1)) * RW * RY, &maps->roc2, xg, yg, t - D, &bars[k]);
+      }
+    }
+  };
+  if constexpr (TMA) {
+    if (tid == 0) {
+      for (int k = 0; k < NB; k++) mbar_init(&bars[k], 1);
+      mbar_init_fence();
+    }
+    __syncthreads();
+    if (tid == 0)
+      for (int t = s0; t < s0 + NB - 1 && t <= se; t++) tma_issue(t);
+  }
+
   for (int sbase = s0; sbase <= se; sbase += U) {
     static_for<U>([&](auto ph_c) {
       constexpr int PH = decltype(ph_c)::value;
@@ -258,10 +307,33 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
       if (s > se) return;  // uniform over the CTA
       const int soff = s * plane;
 
-      // roc2 (and, for level 1, the old state) of every level, issued before the
-      // level loop so that their latency overlaps the higher levels' arithmetic
+      if constexpr (TMA) {
+        if (tid == 0 && s + NB - 1 <= se) tma_issue(s + NB - 1);
+        if (!mbar_wait(&bars[(s - s0) & (NB - 1)], ((s - s0) / NB) & 1, 1u << 26)) tma_timeout = 1;
+      }
+      // roc2 (and, for level 1, the old state) of every level: from the TMA rings,
+      // or issued before the level loop so that their latency overlaps the higher
+      // levels' arithmetic
       Pack<T, VX> r2c[TO == 2 ? TT : 1][CY], pvc[CY];
-      if constexpr (TO == 2) {
+      if constexpr (TO == 2 && TMA) {
+#pragma unroll
+        for (int l = TT; l >= 1; l--) {
+          const int kr = (s - s0 - (l - 1) * D + NR) & (NR - 1);
+#pragma unroll
+          for (int c = 0; c < CY; c++) {
+            const size_t off = (size_t)(ty + c * NTY) * RW + tx * VX;
+            Pack<ST, VX> raw;
+            raw.load(ring_roc2 + (size_t)kr * RW * RY + off);
+#pragma unroll
+            for (int v = 0; v < VX; v++) r2c[l - 1][c].e[v] = to_compute<T>(raw.e[v], range_bad);
+            if (l == 1) {
+              raw.load(ring_prev + (size_t)((s - s0) & (NB - 1)) * RW * RY + off);
+#pragma unroll
+              for (int v = 0; v < VX; v++) pvc[c].e[v] = to_compute<T>(raw.e[v], range_bad);
+            }
+          }
+        }
+      } else if constexpr (TO == 2) {
 #pragma unroll
         for (int l = TT; l >= 1; l--) {
           const int p = s - l * D;
@@ -365,7 +437,12 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
         Pack<T, VX> in;
 #pragma unroll
         for (int v = 0; v < VX; v++) in.e[v] = T(0);
-        if (s_in && y_dom[c]) {
+        if constexpr (TMA) {
+          Pack<ST, VX> raw;  // out-of-range boxes are zero-filled by the copy
+          raw.load(ring_cur + (size_t)((s - s0) & (NB - 1)) * RW * RY + (size_t)(ty + c * NTY) * RW + tx * VX);
+#pragma unroll
+          for (int v = 0; v < VX; v++) in.e[v] = to_compute<T>(raw.e[v], range_bad);
+        } else if (s_in && y_dom[c]) {
           if (xg_dom) {
             in.ldg(a.cur + soff + col[c], range_bad);
           } else {
@@ -399,20 +476,34 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
   if constexpr (std::is_same<T, Df64>::value) {
     if (range_bad && a.range_flag) atomicOr(a.range_flag, 1u);
   }
+  if constexpr (TMA) {
+    if (tma_timeout && a.range_flag) atomicOr(a.range_flag, 2u);  // a copy never completed
+  }
 }
 
 template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX>
 __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<typename StorageOf<T>::type> a) {
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   fused_tile<OP, T, COMP, TT, NTX, NTY, CY, VX>(a, blockIdx.x, blockIdx.y, blockIdx.z, threadIdx.x, threadIdx.y,
                                                 smraw);
 }
 
+// The same pass with the input planes staged by TMA; the tensor maps travel as
+// grid constants.
 template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX>
+__global__ void __launch_bounds__(NTX *NTY)
+    fused_pass_tma(FusedArgs<typename StorageOf<T>::type> a, const __grid_constant__ TmaMaps maps) {
+  extern __shared__ __align__(128) unsigned char smraw[];
+  fused_tile<OP, T, COMP, TT, NTX, NTY, CY, VX, true>(a, blockIdx.x, blockIdx.y, blockIdx.z, threadIdx.x,
+                                                      threadIdx.y, smraw, &maps);
+}
+
+template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX, bool TMA>
 cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
-  using S = FusedShape<OP, T, COMP, TT, NTX, NTY, CY, VX>;
+  using S = FusedShape<OP, T, COMP, TT, NTX, NTY, CY, VX, TMA>;
   constexpr int R = S::R, BX = S::BX, BY = S::BY;
-  auto kern = fused_pass<OP, T, COMP, TT, NTX, NTY, CY, VX>;
+  auto kern = TMA ? (void *)fused_pass_tma<OP, T, COMP, TT, NTX, NTY, CY, VX>
+                  : (void *)fused_pass<OP, T, COMP, TT, NTX, NTY, CY, VX>;
   const size_t smem = S::smem_bytes;
   static bool attr_set = false;  // per instantiation, host side
   if (!attr_set) {
@@ -460,19 +551,26 @@ cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
   a.range_flag = L.range_flag;
   a.zchunk = zchunk;
   a.write_prev = L.write_prev;
-  kern<<<dim3(gx, gy, nz_ch), dim3(NTX, NTY), smem, s>>>(a);
+  if constexpr (TMA) {
+    if (!L.tma_cur || !L.tma_roc2 || !L.tma_prev) return cudaErrorInvalidValue;
+    TmaMaps maps;
+    maps.cur = *static_cast<const CUtensorMap *>(L.tma_cur);
+    maps.prev = *static_cast<const CUtensorMap *>(L.tma_prev);
+    maps.roc2 = *static_cast<const CUtensorMap *>(L.tma_roc2);
+    fused_pass_tma<OP, T, COMP, TT, NTX, NTY, CY, VX><<<dim3(gx, gy, nz_ch), dim3(NTX, NTY), smem, s>>>(a, maps);
+  } else {
+    fused_pass<OP, T, COMP, TT, NTX, NTY, CY, VX><<<dim3(gx, gy, nz_ch), dim3(NTX, NTY), smem, s>>>(a);
+  }
   return cudaGetLastError();
 }
 
-template <int OP, class T, bool COMP, int NTX, int NTY, int CY, int VX, int TMAX>
+template <int OP, class T, bool COMP, int NTX, int NTY, int CY, int VX, int TMAX, bool TMA = false>
 cudaError_t launch_variant(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
   switch (L.steps) {
-    case 1: return launch_tt<OP, T, COMP, 1, NTX, NTY, CY, VX>(g, L, s);
-    case 2: if constexpr (TMAX >= 2) return launch_tt<OP, T, COMP, 2, NTX, NTY, CY, VX>(g, L, s); break;
-    case 3: if constexpr (TMAX >= 3) return launch_tt<OP, T, COMP, 3, NTX, NTY, CY, VX>(g, L, s); break;
-    case 4: if constexpr (TMAX >= 4) return launch_tt<OP, T, COMP, 4, NTX, NTY, CY, VX>(g, L, s); break;
-    case 5: if constexpr (TMAX >= 5) return launch_tt<OP, T, COMP, 5, NTX, NTY, CY, VX>(g, L, s); break;
-    case 6: if constexpr (TMAX >= 6) return launch_tt<OP, T, COMP, 6, NTX, NTY, CY, VX>(g, L, s); break;
+    case 1: return launch_tt<OP, T, COMP, 1, NTX, NTY, CY, VX, TMA>(g, L, s);
+    case 2: if constexpr (TMAX >= 2) return launch_tt<OP, T, COMP, 2, NTX, NTY, CY, VX, TMA>(g, L, s); break;
+    case 3: if constexpr (TMAX >= 3) return launch_tt<OP, T, COMP, 3, NTX, NTY, CY, VX, TMA>(g, L, s); break;
+    case 4: if constexpr (TMAX >= 4) return launch_tt<OP, T, COMP, 4, NTX, NTY, CY, VX, TMA>(g, L, s); break;
   }
   return cudaErrorInvalidValue;
 }
@@ -487,15 +585,21 @@ template <int OP, class T, bool COMP>
 cudaError_t launch_fused_op_impl(const Geom &g, const FusedConfig &cfg, const FusedLaunch &L,
                                  cudaStream_t s) {
   constexpr int TM = fused_tmax<OP, T>();
+  // TMA variants (2, 3) are built for FP32 storage, where the rings fit shared memory
+  constexpr bool kTma = std::is_same<T, float>::value;
   if constexpr (OpTraits<OP>::R == 1) {  // x pairs: vector loads, stores and shared-memory traffic
     switch (cfg.variant) {
       case 0: return launch_variant<OP, T, COMP, 32, 16, 2, 2, TM>(g, L, s);  // 64 x 32 region, 512 threads
       case 1: return launch_variant<OP, T, COMP, 16, 64, 1, 2, TM>(g, L, s);  // 32 x 64 region, 1024 threads
+      case 2: if constexpr (kTma) return launch_variant<OP, T, COMP, 32, 16, 2, 2, TM, true>(g, L, s); break;
+      case 3: if constexpr (kTma) return launch_variant<OP, T, COMP, 16, 64, 1, 2, TM, true>(g, L, s); break;
     }
   } else {  // radius 4: 10-plane queues leave no registers for pairs
     switch (cfg.variant) {
       case 0: return launch_variant<OP, T, COMP, 64, 16, 2, 1, TM>(g, L, s);  // 64 x 32 region, 1024 threads
       case 1: return launch_variant<OP, T, COMP, 32, 32, 2, 1, TM>(g, L, s);  // 32 x 64 region, 1024 threads
+      case 2: if constexpr (kTma) return launch_variant<OP, T, COMP, 64, 16, 2, 1, TM, true>(g, L, s); break;
+      case 3: if constexpr (kTma) return launch_variant<OP, T, COMP, 32, 32, 2, 1, TM, true>(g, L, s); break;
     }
   }
   return cudaErrorInvalidValue;

@@ -219,6 +219,48 @@ void drop_graph(girih_gpu_ctx *c) {
   c->g_steps = -1;
 }
 
+// TMA tensor map of a device-layout array (3-D: x pitch, rows, planes) with the
+// box of a TMA variant; encoded once per (array, variant) and kept in the context.
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+    cudaGetLastError();
+  }
+  return fn;
+}
+
+const CUtensorMap *tensor_map(girih_gpu_ctx *c, int arr, const void *base) {
+  const int v = c->fcfg.variant - 2;
+  if (v < 0 || v > 1) return nullptr;
+  if (!c->tmap_ok[arr][v]) {
+    EncodeTiledFn fn = encode_tiled();
+    if (!fn) return nullptr;
+    const Geom &g = c->g;
+    const cuuint64_t dims[3] = {(cuuint64_t)g.px, (cuuint64_t)g.nny, (cuuint64_t)g.nnz};
+    const cuuint64_t strides[2] = {(cuuint64_t)g.px * c->tsz, (cuuint64_t)g.px * g.nny * c->tsz};
+    const cuuint32_t box[3] = {(cuuint32_t)c->fcfg.box_w, (cuuint32_t)c->fcfg.box_h, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(&c->tmaps[arr][v], c->tsz == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                    3, const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return nullptr;
+    c->tmap_ok[arr][v] = true;
+  }
+  return &c->tmaps[arr][v];
+}
+
 // Extra field buffers for the fused schedule: inputs and outputs of a fused
 // pass must differ because neighbouring tiles read overlapping halos.
 int ensure_fused_buffers(girih_gpu_ctx *c) {
@@ -281,6 +323,13 @@ int issue_steps_impl(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *
     // time order 1 never reads state t-1, so only the last pass writes it (U1)
     L.write_prev = (c->g.to == 2 || left == T) ? 1 : 0;
     L.range_flag = reinterpret_cast<unsigned *>(c->acc + 6);
+    if (c->fcfg.variant >= 2) {
+      L.tma_prev = tensor_map(c, *iu1, c->f[*iu1]);
+      L.tma_cur = tensor_map(c, *iu2, c->f[*iu2]);
+      L.tma_roc2 = c->g.to == 2 ? tensor_map(c, 4, c->roc2) : L.tma_cur;
+      if (!L.tma_prev || !L.tma_cur || !L.tma_roc2)
+        return fail(GIRIH_GPU_ECUDA, "TMA tensor map encoding failed");
+    }
     for (int m = 0; m < 5; m++) L.cc[m] = c->cc[m];
     cudaError_t e = launch_fused(c->g, c->tsz, c->d.precision, c->fcfg, L, st);
     if (e != cudaSuccess) return fail(GIRIH_GPU_ECUDA, std::string("fused launch: ") + cudaGetErrorString(e));
@@ -554,7 +603,8 @@ int girih_gpu_run(girih_gpu_ctx *c, int nt, float *ms_out) {
     c->g_new_iu1 = a;
     c->g_new_iu2 = b;
   }
-  const bool df = c->d.precision == GIRIH_FP64_DF && c->sched == GIRIH_SCHED_FUSED;
+  const bool df = c->sched == GIRIH_SCHED_FUSED &&
+                  (c->d.precision == GIRIH_FP64_DF || c->fcfg.variant >= 2);  // kernels that report through the flag
   unsigned *range_flag = reinterpret_cast<unsigned *>(c->acc + 6);
   if (df) CK(cudaMemsetAsync(range_flag, 0, sizeof(unsigned), c->st));
   CK(cudaEventRecord(c->e0, c->st));
@@ -571,6 +621,7 @@ int girih_gpu_run(girih_gpu_ctx *c, int nt, float *ms_out) {
     if (bad) {
       c->iu1 = c->g_new_iu1;
       c->iu2 = c->g_new_iu2;
+      if (bad & 2u) return fail(GIRIH_GPU_ETIMEOUT, "a TMA plane copy did not complete within the wait bound");
       return fail(GIRIH_GPU_ERANGE, "a field value left the FP32 exponent range of the double-float fused kernel; "
                                     "use GIRIH_FP64 for this grid");
     }

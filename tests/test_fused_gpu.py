@@ -189,3 +189,31 @@ def test_fused_double_float_reports_range_overflow():
         with pytest.raises(gpu.GirihGpuError) as e:
             ctx.run(2)
         assert e.value.code == 8
+
+
+@pytest.mark.parametrize("op", FUSED_OPS)
+@pytest.mark.parametrize("precision", ["fp32", "mixed"])
+@pytest.mark.parametrize("variant", [2, 3])
+def test_fused_tma_variants(op, precision, variant):
+    """Input planes staged into shared memory by TMA (cp.async.bulk.tensor):
+    same results as the register/global-load variants, every depth, including
+    grids smaller than one box and boxes hanging over every domain edge."""
+    r = gpu.OP_INFO[op][0]
+    w, h = TILE[variant - 2]
+    for shape in (_shape(op), (5, 3, 4), (70, 2, 9)):
+        g0 = oracle_grid(op, *shape, seed=23)
+        nt = 7
+        ref = g0.copy().run(nt, nthreads=4)
+        for depth in range(1, MAX_DEPTH[(precision, r)] + 1):
+            block = (w - 2 * depth * r - 3, h - 2 * depth * r)  # FP32 boxes start on 16 bytes: 4 columns
+            with gpu_context(g0.copy(), precision=precision, schedule="fused", fusion_depth=depth,
+                             block=block) as ctx:
+                with gpu_context(g0.copy(), precision=precision, schedule="fused", fusion_depth=depth,
+                                 block=_block(op, depth, variant - 2)) as plain_ctx:
+                    ctx.run(nt)
+                    plain_ctx.run(nt)
+                    u1, u2 = ctx.download()
+                    p1, p2 = plain_ctx.download()
+            np.testing.assert_array_equal(u1, p1)  # same arithmetic, different data movement
+            np.testing.assert_array_equal(u2, p2)
+            assert max_rel(u1, ref.U1, ref) < 5e-6

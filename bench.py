@@ -172,9 +172,11 @@ def run_ours(args, wl, rank, world, local):
     sampler = ClockSampler(local)
     with sampler:
         for name, kw in forms.items():
-            ctx = gpu.Context(op, n, n, n, device=local, fusion_depth=args.depth if kw["schedule"] == "fused" else 0, **kw)
+            blk = tuple(int(x) for x in args.block.split(",")) if args.block and kw["schedule"] == "fused" else (0, 0)
+            ctx = gpu.Context(op, n, n, n, device=local, fusion_depth=args.depth if kw["schedule"] == "fused" else 0,
+                              block=blk, **kw)
             ctx.fill_seeded(wl["seed"], wl["f"], wl["roc2"], (0.0, 0.0), coefs=wl["coefs"], f32_exact=True)
-            if kw["schedule"] != "plain" and not args.depth:
+            if kw["schedule"] != "plain" and not args.depth and not args.block:
                 ctx.autotune()  # picks tile and fusion depth on this grid; the grid state is restored
             for _ in range(args.warmup):
                 ctx.run(nt)
@@ -421,6 +423,7 @@ def main():
     ap.add_argument("--forms", default="")
     ap.add_argument("--headline", default="mixed")
     ap.add_argument("--depth", type=int, default=0)
+    ap.add_argument("--block", default="", help="fused output tile BX,BY (selects the tile variant)")
     ap.add_argument("--grid", "--n", dest="n", type=int, default=0,
                     help="override the grid edge (small profiling cases)")
     ap.add_argument("--nt", type=int, default=0, help="override the number of time steps")

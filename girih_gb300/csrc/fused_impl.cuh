@@ -366,6 +366,15 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
 #pragma unroll
         for (int c = 0; c < CY; c++) {
           const T *srow = thr + ((RB * TT + (L - 1)) * PR + c * NTY) * PW;
+          T val[VX];
+          // rows outside level L's valid band (or halo planes) only carry their
+          // value: a warp covers whole rows, so this branch is warp-uniform except
+          // at the two x edges of the region
+          const bool row_on = p_int && ((act >> (((L - 1) * CY + c) * VX)) & ((1u << VX) - 1));
+          if (!row_on) {
+#pragma unroll
+            for (int v = 0; v < VX; v++) val[v] = q[L - 1][c][v][SL];
+          } else {
           T yv[2 * R][VX];
 #pragma unroll
           for (int d = 1; d <= R; d++) {
@@ -378,7 +387,6 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
               yv[R + d - 1][v] = dn.e[v];
             }
           }
-          T val[VX];
           static_for<VX>([&](auto v_c) {
             constexpr int V = decltype(v_c)::value;
             const T centre = q[L - 1][c][V][SL];
@@ -409,6 +417,7 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
             }
             val[V] = on ? cand : centre;  // halo and out-of-region points keep their value
           });
+          }
           if constexpr (L == TT || L == TT - 1) {
             if (p_out && y_outr[c] && (L == TT || a.write_prev)) {
               ST *dst = (L == TT ? a.out_cur : a.out_prev) + poff + col[c];

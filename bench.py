@@ -38,6 +38,9 @@ WORKLOADS = {
     "star7_jacobi_512": dict(op=1, n=512, nt=500, seed=1, f=(0.0, 1.0), roc2=(0.0, 0.0), coefs=[-0.28472, 0.16]),
     "star25_leapfrog_480": dict(op=0, n=480, nt=200, seed=2, f=(-1.0, 1.0), roc2=(0.05, 0.15),
                                 coefs=[-8.541667, 1.6, -0.2, 0.025396826, -0.0017857143]),
+    # variable coefficients, coefficient arrays U(0.01, 0.1/radius)
+    "var7_384": dict(op=5, n=384, nt=200, seed=3, f=(0.0, 1.0), roc2=(0.0, 0.0), c=(0.01, 0.1), coefs=None),
+    "var25_384": dict(op=4, n=384, nt=200, seed=3, f=(0.0, 1.0), roc2=(0.0, 0.0), c=(0.01, 0.025), coefs=None),
 }
 
 
@@ -135,12 +138,10 @@ def pass_bytes(op_info, tsz, schedule, precision):
     """Compulsory HBM bytes per grid point of one kernel launch.
     plain: read v (+u, roc2), write u.  fused: read cur (+prev, roc2), write two states."""
     r, to, nc, var = op_info
+    cb = nc * (2 if precision == "mixed" else tsz) if var else 0  # coefficient arrays, read once per launch
     if schedule == "plain":
-        b = 2 * tsz + (2 * tsz if to == 2 else 0)
-        if var:
-            b += nc * (2 if precision == "mixed" else tsz)
-        return b
-    return (3 * tsz + 2 * tsz) if to == 2 else (tsz + tsz)
+        return 2 * tsz + (2 * tsz if to == 2 else 0) + cb
+    return ((3 * tsz + 2 * tsz) if to == 2 else (tsz + tsz)) + cb
 
 
 def run_ours(args, wl, rank, world, local):
@@ -151,12 +152,21 @@ def run_ours(args, wl, rank, world, local):
     torch.cuda.set_device(local)
     n, nt, op = wl["n"], wl["nt"], wl["op"]
     lups = float(n) ** 3 * (2 * ((nt + 1) // 2))
-    forms = {
-        "plain64": dict(precision="fp64", schedule="plain"),
-        "fused64": dict(precision="fp64", schedule="fused"),
-        "fused64df": dict(precision="fp64df", schedule="fused"),
-        "mixed": dict(precision="mixed", schedule="fused"),
-    }
+    if gpu.OP_INFO[op][3]:  # variable coefficients: FP32-field forms are fused
+        forms = {
+            "plain64": dict(precision="fp64", schedule="plain"),
+            "mixedplain": dict(precision="mixed", schedule="plain"),
+            "fused32": dict(precision="fp32", schedule="fused"),
+            "mixed": dict(precision="mixed", schedule="fused"),
+        }
+    else:
+        forms = {
+            "plain64": dict(precision="fp64", schedule="plain"),
+            "fused64": dict(precision="fp64", schedule="fused"),
+            "fused64df": dict(precision="fp64df", schedule="fused"),
+            "mixed": dict(precision="mixed", schedule="fused"),
+        }
+    crange = wl.get("c", (0.0, 0.0))
     if args.forms:
         forms = {k: v for k, v in forms.items() if k in args.forms.split(",")}
     dist = world > 1
@@ -175,7 +185,7 @@ def run_ours(args, wl, rank, world, local):
             blk = tuple(int(x) for x in args.block.split(",")) if args.block and kw["schedule"] == "fused" else (0, 0)
             ctx = gpu.Context(op, n, n, n, device=local, fusion_depth=args.depth if kw["schedule"] == "fused" else 0,
                               block=blk, **kw)
-            ctx.fill_seeded(wl["seed"], wl["f"], wl["roc2"], (0.0, 0.0), coefs=wl["coefs"], f32_exact=True)
+            ctx.fill_seeded(wl["seed"], wl["f"], wl["roc2"], crange, coefs=wl["coefs"], f32_exact=True)
             if kw["schedule"] != "plain" and not args.depth and not args.block:
                 ctx.autotune()  # picks tile and fusion depth on this grid; the grid state is restored
             for _ in range(args.warmup):
@@ -201,14 +211,14 @@ def run_ours(args, wl, rank, world, local):
     errors = {}
     if "plain64" in forms and not args.no_error:
         ref = gpu.Context(op, n, n, n, device=local, precision="fp64", schedule="plain")
-        ref.fill_seeded(wl["seed"], wl["f"], wl["roc2"], (0.0, 0.0), coefs=wl["coefs"], f32_exact=True)
+        ref.fill_seeded(wl["seed"], wl["f"], wl["roc2"], crange, coefs=wl["coefs"], f32_exact=True)
         ref.run(nt)
         for name, kw in forms.items():
             if name == "plain64":
                 continue
             c = gpu.Context(op, n, n, n, device=local, fusion_depth=args.depth if kw["schedule"] == "fused" else 0, **kw)
             # creation picks up the autotuned choice cached above for this operator and size
-            c.fill_seeded(wl["seed"], wl["f"], wl["roc2"], (0.0, 0.0), coefs=wl["coefs"], f32_exact=True)
+            c.fill_seeded(wl["seed"], wl["f"], wl["roc2"], crange, coefs=wl["coefs"], f32_exact=True)
             c.run(nt)
             mr, l2 = gpu.rel_errors(c.compare(ref))
             errors[name] = {"max_rel": mr, "l2_rel": l2, "nt": nt, "against": "plain64 (FP64, parity-checked vs the oracle)"}
@@ -234,30 +244,37 @@ def run_ours(args, wl, rank, world, local):
         host = [torch.empty(shape, dtype=torch.float64, pin_memory=True) for _ in range(3)]
         # fill the host arrays with the seeded inputs: download the initial state
         init = gpu.Context(op, n, n, n, device=local, precision="fp64", schedule="plain")
-        init.fill_seeded(wl["seed"], wl["f"], wl["roc2"], (0.0, 0.0), coefs=wl["coefs"], f32_exact=True)
+        init.fill_seeded(wl["seed"], wl["f"], wl["roc2"], crange, coefs=wl["coefs"], f32_exact=True)
         init.download(host[0].data_ptr(), host[1].data_ptr())
         init.download_roc2(host[2].data_ptr()) if op_info[1] == 2 else None
         init.close()
-        coefs = np.array(wl["coefs"] + [0.0] * (11 - len(wl["coefs"])))
+        if op_info[3]:
+            # coefficient arrays: seeded host values in the workload's range (uploaded every step)
+            rng = np.random.default_rng(wl["seed"])
+            coefs = torch.empty((op_info[2],) + tuple(shape), dtype=torch.float64, pin_memory=True)
+            coefs.numpy()[...] = rng.uniform(*crange, size=coefs.shape)
+        else:
+            coefs = np.array(wl["coefs"] + [0.0] * (11 - len(wl["coefs"])))
         ctx.close()
         ectx = gpu.Context(op, n, n, n, device=local, fusion_depth=args.depth if forms[head]["schedule"] == "fused" else 0,
                            **forms[head])
         u3 = host[2].data_ptr() if op_info[1] == 2 else None
         for _ in range(max(1, args.warmup)):
-            ectx.upload(host[0].data_ptr(), host[1].data_ptr(), u3, coefs)
+            ectx.upload(host[0].data_ptr(), host[1].data_ptr(), u3, coefs if not op_info[3] else coefs.data_ptr())
             ectx.run(nt)
             ectx.download(host[0].data_ptr(), None)
         barrier_sync()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            ectx.upload(host[0].data_ptr(), host[1].data_ptr(), u3, coefs)
+            ectx.upload(host[0].data_ptr(), host[1].data_ptr(), u3, coefs if not op_info[3] else coefs.data_ptr())
             ectx.run(nt)
             ectx.download(host[0].data_ptr(), None)
         barrier_sync()
         wall = max_over_ranks(time.perf_counter() - t0, "cuda")
         nbytes = host[0].numel() * 8
         e2e = {"value": world * args.steps * lups / wall / 1e9, "unit": "GLUP/s",
-               "h2d_bytes_per_step": nbytes * (3 if u3 else 2), "d2h_bytes_per_step": nbytes,
+               "h2d_bytes_per_step": nbytes * (3 if u3 else 2) + (nbytes * op_info[2] if op_info[3] else 0),
+               "d2h_bytes_per_step": nbytes,
                "host_arrays": "pinned FP64 (reference real_t=double layout)"}
         ectx.close()
     for c in ctxs.values():
@@ -374,7 +391,7 @@ def cpu_baseline(wl, seconds, steps=None):
     n, op = wl["n"], wl["op"]
     threads = os.cpu_count() or 1
     g = oracle.Grid(op, n, n, n)
-    g.fill_seeded(wl["seed"], wl["f"], wl["roc2"], coefs=wl["coefs"], nthreads=threads)
+    g.fill_seeded(wl["seed"], wl["f"], wl["roc2"], wl.get("c", (0.0, 0.0)), coefs=wl["coefs"], nthreads=threads)
     t0 = time.perf_counter()
     g.run(2, nthreads=threads)
     per_pair = time.perf_counter() - t0

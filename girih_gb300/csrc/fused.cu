@@ -6,13 +6,17 @@
 namespace girih {
 
 bool fused_supported(const Geom &g, int precision) {
-  (void)precision;
   // the fused kernels index with 32-bit element offsets
-  return (g.op == 0 || g.op == 1 || g.op == 8) && g.elems < ((int64_t)1 << 31);
+  if (g.elems >= ((int64_t)1 << 31)) return false;
+  if (g.op == 0 || g.op == 1 || g.op == 8) return true;
+  // variable coefficients: FP32 fields (FP32 or BF16 coefficients); their FP64
+  // form is bound by the FP64 pipe, where fusion cannot help
+  return (g.op >= 2 && g.op <= 5) && (precision == GIRIH_FP32 || precision == GIRIH_MIXED);
 }
 
 int fused_max_depth(const Geom &g, int precision) {
   if (g.r == 4) return 2;
+  if (g.var) return 3;
   if (precision == GIRIH_FP64_DF) return 3;
   return precision == GIRIH_FP64 ? 2 : 4;
 }
@@ -40,7 +44,7 @@ FusedConfig make_fused_config(const Geom &g, int precision, int depth, int varia
   // rings of the TMA variants, must fit one CTA (227 KiB)
   const size_t tsz = (precision == GIRIH_FP64 || precision == GIRIH_FP64_DF) ? 8 : 4;
   const bool tma = variant >= 2;
-  if (tma && tsz != 4) return c;  // TMA variants are built for FP32 storage
+  if (tma && (tsz != 4 || g.var)) return c;  // TMA variants: FP32 storage, constant coefficients
   const int rp = (g.r + vx - 1) / vx * vx;
   size_t smem = (size_t)2 * depth * (ntx + 2 * rp) * (ry + 2 * g.r) * tsz;
   int align = vx;
@@ -85,7 +89,12 @@ cudaError_t launch_fused(const Geom &g, int tsz, int precision, const FusedConfi
     }
     return cudaErrorInvalidValue;
   }
+  const bool bf16 = precision == GIRIH_MIXED && g.var;
   switch (g.op) {
+    case 2: return bf16 ? launch_fused_op<2, float, true>(g, cfg, L, s) : launch_fused_op<2, float, false>(g, cfg, L, s);
+    case 3: return bf16 ? launch_fused_op<3, float, true>(g, cfg, L, s) : launch_fused_op<3, float, false>(g, cfg, L, s);
+    case 4: return bf16 ? launch_fused_op<4, float, true>(g, cfg, L, s) : launch_fused_op<4, float, false>(g, cfg, L, s);
+    case 5: return bf16 ? launch_fused_op<5, float, true>(g, cfg, L, s) : launch_fused_op<5, float, false>(g, cfg, L, s);
     case 1:
       return tsz == 8 ? launch_fused_op<1, double, false>(g, cfg, L, s)
                       : launch_fused_op<1, float, false>(g, cfg, L, s);

@@ -36,6 +36,8 @@ struct FusedLaunch {
   unsigned *range_flag;    // bit 0: a value left the FP32 exponent range (double-float);
                            // bit 1: a TMA copy did not complete within the wait bound
   const void *tma_cur, *tma_prev, *tma_roc2;  // host CUtensorMap objects (TMA variants)
+  const void *coef;        // variable coefficients (device layout arrays)
+  const float *cscale;     // per-array scales of BF16 coefficients (mixed form)
 };
 
 bool fused_supported(const Geom &g, int precision);
@@ -61,6 +63,14 @@ GIRIH_FUSED_SPEC(8, float, true)
 GIRIH_FUSED_SPEC(0, double, false)
 GIRIH_FUSED_SPEC(0, float, false)
 GIRIH_FUSED_SPEC(0, float, true)
+GIRIH_FUSED_SPEC(2, float, false)
+GIRIH_FUSED_SPEC(2, float, true)
+GIRIH_FUSED_SPEC(3, float, false)
+GIRIH_FUSED_SPEC(3, float, true)
+GIRIH_FUSED_SPEC(4, float, false)
+GIRIH_FUSED_SPEC(4, float, true)
+GIRIH_FUSED_SPEC(5, float, false)
+GIRIH_FUSED_SPEC(5, float, true)
 struct Df64;
 GIRIH_FUSED_SPEC(1, Df64, false)
 GIRIH_FUSED_SPEC(8, Df64, false)

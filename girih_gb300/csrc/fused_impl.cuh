@@ -40,6 +40,8 @@ template <class S> struct FusedArgs {
   int zchunk;
   int write_prev;
   unsigned *range_flag;  // Df64 compute: set when a value leaves the FP32 exponent range
+  const void *coef;      // variable coefficients: nc arrays of g.elems (S, or BF16 in the mixed form)
+  const float *cscale;   // per-array scales of BF16 coefficients
 };
 
 // Storage type of a compute type.
@@ -250,6 +252,15 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
   T cc[5];
 #pragma unroll
   for (int m = 0; m < 5; m++) cc[m] = coef_to_compute<T>(a.cc[m]);
+  // variable coefficients (operators 2-5): full precision, or BF16 with a
+  // per-array scale in the mixed form (COMP selects BF16 for these operators)
+  constexpr bool VAR = OpTraits<OP>::VAR;
+  using CoefF = typename std::conditional<VAR && COMP, CoefBF16, CoefFull<T>>::type;
+  CoefF coeff{};
+  if constexpr (VAR) {
+    if constexpr (COMP) coeff = CoefBF16{static_cast<const __nv_bfloat16 *>(a.coef), g.elems, a.cscale};
+    else coeff = CoefFull<T>{static_cast<const T *>(a.coef), g.elems};
+  }
 
   T q[TT][CY][VX][QL];
 #pragma unroll
@@ -411,6 +422,11 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
                 CoefFull<T> none{nullptr, 0};
                 cand = apply_op<OP, FastArith>(cc, none, 0, acc, uold, r2);
               }
+            } else if constexpr (VAR) {
+              // coefficients exist at interior points only: inactive points
+              // (halo, outside the level's band or plane range) read element 0
+              const int ci = on ? poff + col[c] + V : 0;
+              cand = apply_op<OP, FastArith>(cc, coeff, (int64_t)ci, acc, T(0), T(0));
             } else {
               CoefFull<T> none{nullptr, 0};
               cand = apply_op<OP, FastArith>(cc, none, 0, acc, T(0), T(0));
@@ -558,6 +574,8 @@ cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
   a.out_cur = static_cast<ST *>(L.out_cur);
   for (int m = 0; m < 5; m++) a.cc[m] = L.cc[m];
   a.range_flag = L.range_flag;
+  a.coef = L.coef;
+  a.cscale = L.cscale;
   a.zchunk = zchunk;
   a.write_prev = L.write_prev;
   if constexpr (TMA) {
@@ -587,6 +605,7 @@ cudaError_t launch_variant(const Geom &g, const FusedLaunch &L, cudaStream_t s) 
 // Maximum fusion depth instantiated per operator radius and element type.
 template <int OP, class T> constexpr int fused_tmax() {
   if constexpr (std::is_same<T, Df64>::value) return OpTraits<OP>::R == 4 ? 2 : 3;
+  if constexpr (OpTraits<OP>::VAR) return OpTraits<OP>::R == 4 ? 2 : 3;
   return OpTraits<OP>::R == 4 ? 2 : (sizeof(T) == 8 ? 2 : 4);
 }
 
@@ -594,8 +613,9 @@ template <int OP, class T, bool COMP>
 cudaError_t launch_fused_op_impl(const Geom &g, const FusedConfig &cfg, const FusedLaunch &L,
                                  cudaStream_t s) {
   constexpr int TM = fused_tmax<OP, T>();
-  // TMA variants (2, 3) are built for FP32 storage, where the rings fit shared memory
-  constexpr bool kTma = std::is_same<T, float>::value;
+  // TMA variants (2, 3) are built for FP32 storage, where the rings fit shared
+  // memory, and for the constant-coefficient operators
+  constexpr bool kTma = std::is_same<T, float>::value && !OpTraits<OP>::VAR;
   if constexpr (OpTraits<OP>::R == 1) {  // x pairs: vector loads, stores and shared-memory traffic
     switch (cfg.variant) {
       case 0: return launch_variant<OP, T, COMP, 32, 16, 2, 2, TM>(g, L, s);  // 64 x 32 region, 512 threads

@@ -1,0 +1,10 @@
+// Instantiation of the time-fused kernel for operator 5 (variable coefficients), FP32 fields, FP32 coefficients.
+#include "fused_impl.cuh"
+
+namespace girih {
+template <>
+cudaError_t launch_fused_op<5, float, false>(const Geom &g, const FusedConfig &cfg, const FusedLaunch &L,
+                                          cudaStream_t s) {
+  return launch_fused_op_impl<5, float, false>(g, cfg, L, s);
+}
+}  // namespace girih

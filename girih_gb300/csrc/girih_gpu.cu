@@ -323,6 +323,8 @@ int issue_steps_impl(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *
     // time order 1 never reads state t-1, so only the last pass writes it (U1)
     L.write_prev = (c->g.to == 2 || left == T) ? 1 : 0;
     L.range_flag = reinterpret_cast<unsigned *>(c->acc + 6);
+    L.coef = c->coef;
+    L.cscale = c->scale;
     if (c->fcfg.variant >= 2) {
       L.tma_prev = tensor_map(c, *iu1, c->f[*iu1]);
       L.tma_cur = tensor_map(c, *iu2, c->f[*iu2]);
@@ -427,6 +429,11 @@ int girih_gpu_create(girih_gpu_ctx **out, const girih_gpu_desc *d) {
   if (sched != GIRIH_SCHED_PLAIN && untuned && cached_choice(c->g, d->precision, &tc)) {
     if (d->schedule == GIRIH_SCHED_AUTO) c->sched = sched = tc.sched;
     if (tc.sched == GIRIH_SCHED_FUSED) c->fcfg = make_fused_config(c->g, d->precision, tc.depth, tc.variant);
+  } else if (d->schedule == GIRIH_SCHED_AUTO && c->g.var && c->g.r == 4) {
+    // untuned default: at radius 4 the overlapped tiles recompute ~2x the points,
+    // which costs the variable-coefficient operator more than the coefficient
+    // bytes it saves; only a tuning run that measured otherwise selects fusion
+    c->sched = sched = GIRIH_SCHED_PLAIN;
   }
   if (sched == GIRIH_SCHED_FUSED && !c->fcfg.depth) {
     c->fcfg = choose_fused_config(c->g, d->precision, d->fusion_depth, d->block_x, d->block_y);

@@ -16,6 +16,11 @@ struct girih_gpu_ctx {
   void *f[4] = {nullptr, nullptr, nullptr, nullptr};  // field buffers
   int iu1 = 0, iu2 = 1;                               // buffers holding U1 and U2
   void *roc2 = nullptr;
+  // double-float fused form: FP32-pair mirrors of the four field buffers and
+  // roc2, split from the FP64 buffers at the start of each run and joined back
+  // at its end (the FP64 buffers stay the state every other entry point sees)
+  void *dfp[4] = {nullptr, nullptr, nullptr, nullptr};
+  void *dfr2 = nullptr;
   void *coef = nullptr;
   float *scale = nullptr;
   double cc[5] = {0, 0, 0, 0, 0};

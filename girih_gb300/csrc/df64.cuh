@@ -1,20 +1,23 @@
 // Double-float ("df64") arithmetic: a value is an unevaluated sum hi + lo of two
 // FP32 numbers, ~48 significant bits.  GB300 issues FP32 at 64x its FP64 rate,
-// so the fused kernels can keep FP64 data in HBM and do their arithmetic on
-// FP32 pairs.
+// so the fused kernels can carry FP64 fields as FP32 pairs and do their
+// arithmetic on the pairs.
 //
-// Algorithms (published, restated here): Knuth's TwoSum and Dekker's
-// FastTwoSum for error-free addition, and the FMA-based exact product
-// (Ogita, Rump, Oishi, "Accurate sum and dot product", 2005, Alg. 3.1/3.5 and
-// the TwoProduct-by-FMA variant).  Addition is the "sloppy" double-float sum
-// (one TwoSum of the high parts, the low parts added in FP32, renormalised),
-// whose absolute error is ~2^-48 (|a| + |b|).
+// Algorithms (published, restated here): Knuth's TwoSum for error-free
+// addition, Dekker's FastTwoSum for renormalisation, and the FMA-based exact
+// product (Ogita, Rump, Oishi, "Accurate sum and dot product", 2005, Alg. 3.1
+// and the TwoProduct-by-FMA variant).  The operators below defer
+// renormalisation: a sum is TwoSum of the high parts with the low parts and the
+// error term added in FP32 (8 operations), a product keeps the FMA error terms
+// in the low part (4 operations), and df_norm() renormalises once per stencil
+// update (3 operations).  Each operation's absolute error stays ~2^-47 of its
+// operands while the low parts are a few ulps of the high parts.
 #pragma once
 #include <cstdint>
 
 namespace girih {
 
-struct Df64 {
+struct __align__(8) Df64 {
   float hi, lo;
   Df64() = default;
   __host__ __device__ constexpr Df64(float h, float l) : hi(h), lo(l) {}
@@ -36,10 +39,7 @@ __device__ __forceinline__ void df_two_sum(float a, float b, float &s, float &e)
 __device__ __forceinline__ Df64 operator+(Df64 a, Df64 b) {
   float s, e;
   df_two_sum(a.hi, b.hi, s, e);
-  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
-  Df64 r;
-  df_fast_two_sum(s, e, r.hi, r.lo);
-  return r;
+  return Df64(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
 }
 
 __device__ __forceinline__ Df64 operator-(Df64 a) { return Df64(-a.hi, -a.lo); }
@@ -51,8 +51,13 @@ __device__ __forceinline__ Df64 operator*(Df64 a, Df64 b) {
   float e = __fmaf_rn(a.hi, b.hi, -p);  // exact error of the product
   e = __fmaf_rn(a.hi, b.lo, e);
   e = __fmaf_rn(a.lo, b.hi, e);
+  return Df64(p, e);
+}
+
+// Renormalise: |lo| <= ulp(hi)/2.
+__device__ __forceinline__ Df64 df_norm(Df64 a) {
   Df64 r;
-  df_fast_two_sum(p, e, r.hi, r.lo);
+  df_fast_two_sum(a.hi, a.lo, r.hi, r.lo);
   return r;
 }
 

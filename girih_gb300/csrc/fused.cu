@@ -26,8 +26,19 @@ int fused_max_depth(const Geom &g, int precision) {
 //   each), variant 1 = 32 x 64 (16x64 threads, 1 row each);
 //   radius 4 (one column per thread): variant 0 = 64 x 32 (64x16 threads, 2
 //   rows), variant 1 = 32 x 64 (32x32 threads, 2 rows);
-//   variants 2 and 3: 0 and 1 with TMA-staged input planes.
-static void variant_shape(int v, int r, int *ntx, int *ry, int *vx) {
+//   variants 2 and 3: 0 and 1 with TMA-staged input planes;
+//   double-float: one column per thread in variants 0 = 64 x 32 (64x16 threads,
+//   2 rows), 1 = 32 x 32 (32x16 threads, 2 rows), 2 = 64 x 16 (64x16 threads,
+//   1 row); x pairs (radius 1) in variants 3 = 64 x 32 (32x16 threads, 2 rows)
+//   and 4 = 32 x 64 (16x64 threads, 1 row).
+static void variant_shape(int v, int r, int precision, int *ntx, int *ry, int *vx) {
+  if (precision == GIRIH_FP64_DF) {
+    static const int shape[5][3] = {{64, 32, 1}, {32, 32, 1}, {64, 16, 1}, {64, 32, 2}, {32, 64, 2}};
+    *ntx = shape[v][0];
+    *ry = shape[v][1];
+    *vx = shape[v][2];
+    return;
+  }
   *ntx = (v % 2) == 0 ? 64 : 32;
   *ry = (v % 2) == 0 ? 32 : 64;
   *vx = r == 1 ? 2 : 1;
@@ -39,12 +50,14 @@ FusedConfig make_fused_config(const Geom &g, int precision, int depth, int varia
       variant < 0 || variant >= FV_COUNT)
     return c;
   int ntx, ry, vx;
-  variant_shape(variant, g.r, &ntx, &ry, &vx);
+  variant_shape(variant, g.r, precision, &ntx, &ry, &vx);
   // double-buffered shared memory of all levels (rows padded by r), plus the TMA
   // rings of the TMA variants, must fit one CTA (227 KiB)
   const size_t tsz = (precision == GIRIH_FP64 || precision == GIRIH_FP64_DF) ? 8 : 4;
-  const bool tma = variant >= 2;
+  const bool tma = variant >= 2 && precision != GIRIH_FP64_DF;
   if (tma && (tsz != 4 || g.var)) return c;  // TMA variants: FP32 storage, constant coefficients
+  if (precision == GIRIH_FP64_DF && variant >= 2 && g.r != 1) return c;
+  if (precision != GIRIH_FP64_DF && variant == 4) return c;
   const int rp = (g.r + vx - 1) / vx * vx;
   size_t smem = (size_t)2 * depth * (ntx + 2 * rp) * (ry + 2 * g.r) * tsz;
   int align = vx;

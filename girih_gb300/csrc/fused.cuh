@@ -8,7 +8,9 @@ namespace girih {
 // columns (tile + halo of depth*R on every side); each thread owns VX x columns
 // and CY rows of it and streams the whole z range.  Variants 2 and 3 are
 // variants 0 and 1 with the input planes staged into shared memory by TMA.
-enum FusedVariant { FV_64x32_512 = 0, FV_32x64_1024 = 1, FV_64x32_512_TMA = 2, FV_32x64_1024_TMA = 3, FV_COUNT = 4 };
+// Tile variants of the FP32/FP64 forms (the double-float form numbers its own
+// five shapes 0-4, see variant_shape in fused.cu).
+enum FusedVariant { FV_64x32_512 = 0, FV_32x64_1024 = 1, FV_64x32_512_TMA = 2, FV_32x64_1024_TMA = 3, FV_COUNT = 5 };
 
 // TMA ring depths: NB planes of the input (and old) state in flight, NR planes
 // of roc2 (level l reads roc2 (l-1)*(R+1) planes after level 1 did).

@@ -30,8 +30,8 @@
 namespace girih {
 
 // Arguments of one fused pass over one grid.  S is the storage type in HBM
-// (float or double); the kernel computes in T (S itself, or Df64 for FP64
-// storage).
+// (float, double, or Df64 pairs: the double-float form streams FP64 fields as
+// FP32 pairs, split from and joined to FP64 around the run).
 template <class S> struct FusedArgs {
   Geom g;
   const S *prev, *cur, *roc2;
@@ -39,22 +39,22 @@ template <class S> struct FusedArgs {
   double cc[5];
   int zchunk;
   int write_prev;
-  unsigned *range_flag;  // Df64 compute: set when a value leaves the FP32 exponent range
+  unsigned *range_flag;  // error flags (bit 1: a TMA copy timed out)
   const void *coef;      // variable coefficients: nc arrays of g.elems (S, or BF16 in the mixed form)
   const float *cscale;   // per-array scales of BF16 coefficients
 };
 
-// Storage type of a compute type.
+// Storage type of a compute type (every compute type is stored as itself).
 template <class T> struct StorageOf { using type = T; };
-template <> struct StorageOf<Df64> { using type = double; };
 
 // Conversions between storage and compute values.
 template <class T, class S> __device__ __forceinline__ T to_compute(S v, unsigned &bad) {
-  if constexpr (std::is_same<T, Df64>::value) return df_split(v, bad);
+  (void)bad;
+  if constexpr (std::is_same<T, S>::value) return v;
   else return (T)v;
 }
 template <class S, class T> __device__ __forceinline__ S to_storage(T v) {
-  if constexpr (std::is_same<T, Df64>::value) return df_to_double(v);
+  if constexpr (std::is_same<T, S>::value) return v;
   else return (S)v;
 }
 template <class T> __device__ __forceinline__ T coef_to_compute(double c) {
@@ -63,6 +63,16 @@ template <class T> __device__ __forceinline__ T coef_to_compute(double c) {
     return Df64(h, __double2float_rn(c - (double)h));
   } else {
     return (T)c;
+  }
+}
+
+// One element through the read-only path (pairs as one 8-byte load).
+template <class S> __device__ __forceinline__ S ldg_elem(const S *p) {
+  if constexpr (std::is_same<S, Df64>::value) {
+    const float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+    return Df64(v.x, v.y);
+  } else {
+    return __ldg(p);
   }
 }
 
@@ -401,7 +411,8 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
           static_for<VX>([&](auto v_c) {
             constexpr int V = decltype(v_c)::value;
             const T centre = q[L - 1][c][V][SL];
-            const bool on = p_int && (act >> (((L - 1) * CY + c) * VX + V) & 1u);
+            // with one column per thread the row test above already decided
+            const bool on = VX == 1 || (p_int && (act >> (((L - 1) * CY + c) * VX + V) & 1u));
             // double-float arithmetic is ~10x the FP32 work: skip inactive points
             // with a branch there; the FP32/FP64 paths stay branch-free
             constexpr bool heavy = std::is_same<T, Df64>::value;
@@ -411,7 +422,17 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
             }
             FusedAcc<R, T, QL, SL, VX, V> acc{srow, q[L - 1][c], yv};
             T cand;
-            if constexpr (TO == 2) {
+            if constexpr (heavy && !VAR) {
+              const T lap = star_grouped_sum<R, FastArith>(cc, acc);
+              if constexpr (TO == 2) {
+                T uold;
+                if constexpr (L >= 2) uold = q[L - 2][c][V][SL];
+                else uold = pvc[c].e[V];
+                cand = (twice(centre) - uold) + r2c[L - 1][c].e[V] * lap;
+              } else {
+                cand = lap;
+              }
+            } else if constexpr (TO == 2) {
               T uold;
               if constexpr (L >= 2) uold = q[L - 2][c][V][SL];
               else uold = pvc[c].e[V];
@@ -431,7 +452,8 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
               CoefFull<T> none{nullptr, 0};
               cand = apply_op<OP, FastArith>(cc, none, 0, acc, T(0), T(0));
             }
-            val[V] = on ? cand : centre;  // halo and out-of-region points keep their value
+            if constexpr (heavy) val[V] = df_norm(cand);  // inactive points took the branch above
+            else val[V] = on ? cand : centre;  // halo and out-of-region points keep their value
           });
           }
           if constexpr (L == TT || L == TT - 1) {
@@ -473,7 +495,7 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
           } else {
 #pragma unroll
             for (int v = 0; v < VX; v++)
-              if (x_dom[v]) in.e[v] = to_compute<T>(__ldg(a.cur + soff + col[c] + v), range_bad);
+              if (x_dom[v]) in.e[v] = to_compute<T>(ldg_elem(a.cur + soff + col[c] + v), range_bad);
           }
         }
 #pragma unroll
@@ -497,9 +519,6 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
         }
       __syncthreads();
     });
-  }
-  if constexpr (std::is_same<T, Df64>::value) {
-    if (range_bad && a.range_flag) atomicOr(a.range_flag, 1u);
   }
   if constexpr (TMA) {
     if (tma_timeout && a.range_flag) atomicOr(a.range_flag, 2u);  // a copy never completed
@@ -527,8 +546,9 @@ template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX, 
 cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
   using S = FusedShape<OP, T, COMP, TT, NTX, NTY, CY, VX, TMA>;
   constexpr int R = S::R, BX = S::BX, BY = S::BY;
-  auto kern = TMA ? (void *)fused_pass_tma<OP, T, COMP, TT, NTX, NTY, CY, VX>
-                  : (void *)fused_pass<OP, T, COMP, TT, NTX, NTY, CY, VX>;
+  void *kern;
+  if constexpr (TMA) kern = (void *)fused_pass_tma<OP, T, COMP, TT, NTX, NTY, CY, VX>;
+  else kern = (void *)fused_pass<OP, T, COMP, TT, NTX, NTY, CY, VX>;
   const size_t smem = S::smem_bytes;
   static bool attr_set = false;  // per instantiation, host side
   if (!attr_set) {
@@ -616,7 +636,21 @@ cudaError_t launch_fused_op_impl(const Geom &g, const FusedConfig &cfg, const Fu
   // TMA variants (2, 3) are built for FP32 storage, where the rings fit shared
   // memory, and for the constant-coefficient operators
   constexpr bool kTma = std::is_same<T, float>::value && !OpTraits<OP>::VAR;
-  if constexpr (OpTraits<OP>::R == 1) {  // x pairs: vector loads, stores and shared-memory traffic
+  if constexpr (std::is_same<T, Df64>::value) {  // one column per thread: pairs already fill 8 bytes
+    switch (cfg.variant) {
+      case 0: return launch_variant<OP, T, COMP, 64, 16, 2, 1, TM>(g, L, s);  // 64 x 32 region, 1024 threads
+      case 1: return launch_variant<OP, T, COMP, 32, 16, 2, 1, TM>(g, L, s);  // 32 x 32 region, 512 threads
+      case 2:  // 64 x 16 region, 1024 threads (radius 1)
+        if constexpr (OpTraits<OP>::R == 1) return launch_variant<OP, T, COMP, 64, 16, 1, 1, TM>(g, L, s);
+        break;
+      case 3:  // x pairs: 64 x 32 region, 512 threads (radius 1)
+        if constexpr (OpTraits<OP>::R == 1) return launch_variant<OP, T, COMP, 32, 16, 2, 2, TM>(g, L, s);
+        break;
+      case 4:  // x pairs: 32 x 64 region, 1024 threads (radius 1)
+        if constexpr (OpTraits<OP>::R == 1) return launch_variant<OP, T, COMP, 16, 64, 1, 2, TM>(g, L, s);
+        break;
+    }
+  } else if constexpr (OpTraits<OP>::R == 1) {  // x pairs: vector loads, stores and shared-memory traffic
     switch (cfg.variant) {
       case 0: return launch_variant<OP, T, COMP, 32, 16, 2, 2, TM>(g, L, s);  // 64 x 32 region, 512 threads
       case 1: return launch_variant<OP, T, COMP, 16, 64, 1, 2, TM>(g, L, s);  // 32 x 64 region, 1024 threads

@@ -264,9 +264,21 @@ const CUtensorMap *tensor_map(girih_gpu_ctx *c, int arr, const void *base) {
 // Extra field buffers for the fused schedule: inputs and outputs of a fused
 // pass must differ because neighbouring tiles read overlapping halos.
 int ensure_fused_buffers(girih_gpu_ctx *c) {
+  const size_t fb = (size_t)c->g.elems * c->tsz;
   for (int b = 2; b < 4; b++) {
     if (!c->f[b]) {
-      int e = dev_alloc(c, &c->f[b], (size_t)c->g.elems * c->tsz);
+      int e = dev_alloc(c, &c->f[b], fb);
+      if (e) return e;
+    }
+  }
+  if (c->d.precision == GIRIH_FP64_DF) {
+    for (int b = 0; b < 4; b++)
+      if (!c->dfp[b]) {
+        int e = dev_alloc(c, &c->dfp[b], fb);
+        if (e) return e;
+      }
+    if (c->g.to == 2 && !c->dfr2) {
+      int e = dev_alloc(c, &c->dfr2, fb);
       if (e) return e;
     }
   }
@@ -307,6 +319,24 @@ int issue_steps_impl(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *
   }
   // fused: state S-1 in buffer iu1, state S in iu2; each pass writes the two
   // newest states into the two spare buffers
+  const bool dfp = c->d.precision == GIRIH_FP64_DF;
+  void *const *buf = dfp ? c->dfp : c->f;
+  unsigned *flag = reinterpret_cast<unsigned *>(c->acc + 6);
+  if (dfp && steps > 0) {
+    // FP64 -> pairs: both states, the spares (whose halos the passes read), roc2
+    int sp[2], n = 0;
+    for (int b = 0; b < 4 && n < 2; b++)
+      if (b != *iu1 && b != *iu2) sp[n++] = b;
+    cudaError_t e = launch_df_split(c->g, static_cast<const double *>(c->f[*iu1]), c->dfp[*iu1], nullptr, nullptr,
+                                    flag, st);
+    if (e == cudaSuccess)
+      e = launch_df_split(c->g, static_cast<const double *>(c->f[*iu2]), c->dfp[*iu2], c->dfp[sp[0]], c->dfp[sp[1]],
+                          flag, st);
+    if (e == cudaSuccess && c->g.to == 2)
+      e = launch_df_split(c->g, static_cast<const double *>(c->roc2), c->dfr2, nullptr, nullptr, flag, st);
+    if (e != cudaSuccess) return fail(GIRIH_GPU_ECUDA, std::string("double-float split: ") + cudaGetErrorString(e));
+    *launches += c->g.to == 2 ? 3 : 2;
+  }
   int left = steps;
   while (left > 0) {
     int T = std::min(left, c->fcfg.depth);
@@ -314,18 +344,18 @@ int issue_steps_impl(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *
     for (int b = 0; b < 4 && n < 2; b++)
       if (b != *iu1 && b != *iu2) spare[n++] = b;
     FusedLaunch L{};
-    L.prev = c->f[*iu1];
-    L.cur = c->f[*iu2];
-    L.out_prev = c->f[spare[0]];
-    L.out_cur = c->f[spare[1]];
-    L.roc2 = c->roc2;
+    L.prev = buf[*iu1];
+    L.cur = buf[*iu2];
+    L.out_prev = buf[spare[0]];
+    L.out_cur = buf[spare[1]];
+    L.roc2 = dfp ? c->dfr2 : c->roc2;
     L.steps = T;
     // time order 1 never reads state t-1, so only the last pass writes it (U1)
     L.write_prev = (c->g.to == 2 || left == T) ? 1 : 0;
-    L.range_flag = reinterpret_cast<unsigned *>(c->acc + 6);
+    L.range_flag = flag;
     L.coef = c->coef;
     L.cscale = c->scale;
-    if (c->fcfg.variant >= 2) {
+    if (c->fcfg.box_w > 0) {  // TMA variant
       L.tma_prev = tensor_map(c, *iu1, c->f[*iu1]);
       L.tma_cur = tensor_map(c, *iu2, c->f[*iu2]);
       L.tma_roc2 = c->g.to == 2 ? tensor_map(c, 4, c->roc2) : L.tma_cur;
@@ -339,6 +369,12 @@ int issue_steps_impl(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *
     *iu1 = spare[0];
     *iu2 = spare[1];
     left -= T;
+  }
+  if (dfp && steps > 0) {  // pairs -> FP64 (interior points; the halos keep their FP64 values)
+    cudaError_t e = launch_df_join(c->g, c->dfp[*iu1], static_cast<double *>(c->f[*iu1]), st);
+    if (e == cudaSuccess) e = launch_df_join(c->g, c->dfp[*iu2], static_cast<double *>(c->f[*iu2]), st);
+    if (e != cudaSuccess) return fail(GIRIH_GPU_ECUDA, std::string("double-float join: ") + cudaGetErrorString(e));
+    *launches += 2;
   }
   return 0;
 }
@@ -475,6 +511,9 @@ void girih_gpu_destroy(girih_gpu_ctx *c) {
   drop_graph(c);
   for (void *p : c->f)
     if (p) cudaFree(p);
+  for (void *p : c->dfp)
+    if (p) cudaFree(p);
+  if (c->dfr2) cudaFree(c->dfr2);
   if (c->roc2) cudaFree(c->roc2);
   if (c->coef) cudaFree(c->coef);
   if (c->scale) cudaFree(c->scale);
@@ -611,7 +650,7 @@ int girih_gpu_run(girih_gpu_ctx *c, int nt, float *ms_out) {
     c->g_new_iu2 = b;
   }
   const bool df = c->sched == GIRIH_SCHED_FUSED &&
-                  (c->d.precision == GIRIH_FP64_DF || c->fcfg.variant >= 2);  // kernels that report through the flag
+                  (c->d.precision == GIRIH_FP64_DF || c->fcfg.box_w > 0);  // kernels that report through the flag
   unsigned *range_flag = reinterpret_cast<unsigned *>(c->acc + 6);
   if (df) CK(cudaMemsetAsync(range_flag, 0, sizeof(unsigned), c->st));
   CK(cudaEventRecord(c->e0, c->st));
@@ -737,7 +776,7 @@ int girih_gpu_autotune(girih_gpu_ctx *c, int trial_steps, girih_gpu_info_t *chos
   if (cands.empty()) return girih_gpu_info(c, chosen);
   int e = 0;
   if (cands.size() > 1 || cands[0].sched == GIRIH_SCHED_FUSED) {
-    if (!c->f[2] && (e = ensure_fused_buffers(c))) return e;
+    if ((e = ensure_fused_buffers(c))) return e;
     for (int b = 2; b < 4; b++)  // spare buffers carry the fixed halo
       CK(cudaMemcpyAsync(c->f[b], c->f[c->iu2], (size_t)g.elems * c->tsz, cudaMemcpyDeviceToDevice, c->st));
   }

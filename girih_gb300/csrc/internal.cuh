@@ -65,6 +65,13 @@ cudaError_t launch_norms(const Geom &g, const Ta *a, const Tb *bh, const Geom &g
 template <class T>
 cudaError_t launch_seeded(const Geom &g, uint64_t seed, uint32_t stream, double lo, double hi,
                           int round_f32, T *dst_devlayout, double *dst_hostlayout, cudaStream_t s);
+// FP64 fields <-> double-float pairs (8 bytes per point, same layout).  The
+// split writes every element of `in` (halos included) to each non-null output
+// and sets bit 0 of *flag for values outside the FP32 exponent range; the join
+// writes the interior points of `out` only.
+cudaError_t launch_df_split(const Geom &g, const double *in, void *out0, void *out1, void *out2, unsigned *flag,
+                            cudaStream_t s);
+cudaError_t launch_df_join(const Geom &g, const void *in, double *out, cudaStream_t s);
 cudaError_t launch_halo_equal(const Geom &g, const void *a, const void *b, int tsz,
                               unsigned int *flag, cudaStream_t s);
 

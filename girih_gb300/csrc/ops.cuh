@@ -80,6 +80,19 @@ __device__ __forceinline__ T star_const_sum(const T *c, const Vf &V) {
   return s;
 }
 
+// The same sum grouped per distance, c0*v + sum_d c_d*((x_d + y_d) + z_d): two
+// fewer products per distance.  Used where results need not match the
+// reference's association bit for bit (the double-float fused form, held to
+// the FP64 parity bound).
+template <int R, class A, class T, class Vf>
+__device__ __forceinline__ T star_grouped_sum(const T *c, const Vf &V) {
+  T s = A::mul(c[0], V.c());
+#pragma unroll
+  for (int d = 1; d <= R; d++)
+    s = A::add(s, A::mul(c[d], A::add(A::add(GIRIH_PAIR(x, d), GIRIH_PAIR(y, d)), GIRIH_PAIR(z, d))));
+  return s;
+}
+
 // One operator application at the centre point; `uold` is the old value of the
 // updated array (time-order-2 operators), `roc2` the per-point roc2 value.
 template <int OP, class A, class T, class Vf, class Cf>

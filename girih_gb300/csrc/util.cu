@@ -1,6 +1,7 @@
 // Data movement and reduction kernels: layout conversion between the
 // reference's host layout and the device layout, BF16 quantisation, seeded
 // initialisation and the FP64 error norms used by verification.
+#include "df64.cuh"
 #include "internal.cuh"
 
 namespace girih {
@@ -161,6 +162,35 @@ __global__ void halo_equal_kernel(Geom g, const W *__restrict__ a, const W *__re
   }
 }
 
+
+// FP64 -> pairs, two elements per thread (the element count of a device field
+// is even: the row pitch is a multiple of 16 doubles).
+__global__ void df_split_kernel(int64_t n2, const double2 *__restrict__ in, float4 *o0, float4 *o1, float4 *o2,
+                                unsigned *flag) {
+  unsigned bad = 0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n2; t += (int64_t)gridDim.x * blockDim.x) {
+    const double2 d = in[t];
+    const Df64 a = df_split(d.x, bad), b = df_split(d.y, bad);
+    const float4 v = make_float4(a.hi, a.lo, b.hi, b.lo);
+    o0[t] = v;
+    if (o1) o1[t] = v;
+    if (o2) o2[t] = v;
+  }
+  if (bad) atomicOr(flag, 1u);
+}
+
+// pairs -> FP64 at the interior points (x fastest; one row segment per thread group)
+__global__ void df_join_kernel(Geom g, const Df64 *__restrict__ in, double *__restrict__ out) {
+  const int64_t n = (int64_t)g.nx * g.ny * g.nz;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.nx);
+    const int64_t row = t / g.nx;
+    const int j = (int)(row % g.ny), k = (int)(row / g.ny);
+    const int64_t at = g.at(g.r + i, g.r + j, g.r + k);
+    const float2 v = __ldg(reinterpret_cast<const float2 *>(in + at));
+    out[at] = df_to_double(Df64(v.x, v.y));
+  }
+}
 }  // namespace
 
 template <class Tin, class Tout>
@@ -228,5 +258,19 @@ template cudaError_t launch_quantize_bf16<double>(const Geom &, const double *, 
 template cudaError_t launch_quantize_bf16<float>(const Geom &, const float *, __nv_bfloat16 *, const float *, cudaStream_t);
 template cudaError_t launch_seeded<double>(const Geom &, uint64_t, uint32_t, double, double, int, double *, double *, cudaStream_t);
 template cudaError_t launch_seeded<float>(const Geom &, uint64_t, uint32_t, double, double, int, float *, double *, cudaStream_t);
+
+cudaError_t launch_df_split(const Geom &g, const double *in, void *out0, void *out1, void *out2, unsigned *flag,
+                            cudaStream_t s) {
+  const int64_t n2 = g.elems / 2;
+  df_split_kernel<<<grid_for(n2), kThreads, 0, s>>>(n2, reinterpret_cast<const double2 *>(in),
+                                                    static_cast<float4 *>(out0), static_cast<float4 *>(out1),
+                                                    static_cast<float4 *>(out2), flag);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_df_join(const Geom &g, const void *in, double *out, cudaStream_t s) {
+  df_join_kernel<<<grid_for((int64_t)g.nx * g.ny * g.nz), kThreads, 0, s>>>(g, static_cast<const Df64 *>(in), out);
+  return cudaGetLastError();
+}
 
 }  // namespace girih

@@ -155,20 +155,33 @@ def test_autotune_restores_state_and_stays_correct(op, precision, sched):
 
 
 @pytest.mark.parametrize("op", FUSED_OPS)
-@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4])
 def test_fused_double_float_within_fp64_bound(op, variant):
     """FP64 storage, double-float arithmetic: held to the FP64 parity bound."""
     r = gpu.OP_INFO[op][0]
     g0 = oracle_grid(op, *_shape(op), seed=17)
     nt = 9
     ref = g0.copy().run(nt, nthreads=4)
+    # double-float regions: one column per thread (0-2), x pairs (3, 4; one column lost to alignment)
+    w, h, pair = {0: (64, 32, 0), 1: (32, 32, 0), 2: (64, 16, 0), 3: (64, 32, 1), 4: (32, 64, 1)}[variant]
+    if variant >= 2 and r != 1:
+        return  # radius 1 only
     for depth in range(1, (3 if r == 1 else 2) + 1):
+        if h - 2 * depth * r <= 0:
+            continue
         with gpu_context(g0.copy(), precision="fp64df", schedule="fused", fusion_depth=depth,
-                         block=_block(op, depth, variant)) as ctx:
+                         block=(w - 2 * depth * r - pair, h - 2 * depth * r)) as ctx:
             ctx.run(nt)
+            # the passes, plus the FP64 -> pair splits and the pair -> FP64 joins of the run
+            split_join = (3 if gpu.OP_INFO[op][1] == 2 else 2) + 2
+            assert ctx.info()["launches_last_run"] == -(-10 // depth) + split_join
             u1, u2 = ctx.download()
         assert max_rel(u1, ref.U1, ref) <= FP64_TOL, (depth, max_rel(u1, ref.U1, ref))
         assert max_rel(u2, ref.U2, ref) <= FP64_TOL, depth
+        # the FP64 halos are kept bit for bit
+        np.testing.assert_array_equal(u1[:r], g0.U1[:r])
+        np.testing.assert_array_equal(u2[:, :r], g0.U2[:, :r])
+        np.testing.assert_array_equal(u1[:, :, :r], g0.U1[:, :, :r])
 
 
 def test_fused_double_float_reference_init():

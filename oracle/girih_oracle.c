@@ -360,6 +360,26 @@ int go_run(int op, int nx, int ny, int nz, int pnx, int nt, double *U1, double *
   return 0;
 }
 
+int go_run_source(int op, int nx, int ny, int nz, int pnx, int nt, double *U1, double *U2,
+                  const double *U3, const double *coef, const int pt[3], const double *source,
+                  int nsrc, int nthreads) {
+  int r;
+  if (go_op_info(op, &r, 0, 0, 0)) return -1;
+  const int n[3] = {nx, ny, nz};
+  for (int a = 0; a < 3; a++)
+    if (pt[a] < r || pt[a] >= n[a] + r) return -3;
+  const int64_t nny = ny + 2 * r;
+  const int64_t at = IDX(pt[0], pt[1], pt[2]);
+  for (int it = 0; it < nt; it += 2) {
+    int e = go_step(op, nx, ny, nz, pnx, coef, U1, U2, U3, nthreads);
+    if (e) return e;
+    if (it < nsrc) U1[at] += source[it];
+    go_step(op, nx, ny, nz, pnx, coef, U2, U1, U3, nthreads);
+    if (it + 1 < nsrc) U2[at] += source[it + 1];
+  }
+  return 0;
+}
+
 void go_norms(const double *a, const double *b, int nx, int ny, int nz, int pnx, int r,
               double out[4]) {
   const int64_t nny = ny + 2 * r;

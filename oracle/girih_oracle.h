@@ -86,6 +86,16 @@ int go_step(int op, int nx, int ny, int nz, int pnx, const double *coef,
 int go_run(int op, int nx, int ny, int nz, int pnx, int nt,
            double *U1, double *U2, const double *U3, const double *coef, int nthreads);
 
+/* go_run with source-point injection (src/kernels/nb_naive_ts.c:190,196):
+ * after sweep `it` (0-based within this run) the array just updated gets
+ * source[it] added at the point pt = {i, j, k} (array indices, halo included,
+ * like the reference's lsource_pt, src/utils.c:310); sweeps it >= nsrc add
+ * nothing.  pt must be an interior point.  Returns -3 for a point outside the
+ * interior. */
+int go_run_source(int op, int nx, int ny, int nz, int pnx, int nt, double *U1, double *U2,
+                  const double *U3, const double *coef, const int pt[3], const double *source,
+                  int nsrc, int nthreads);
+
 /* Error norms over the interior: out = {max|a-b|, max|b|, sum (a-b)^2, sum b^2}. */
 void go_norms(const double *a, const double *b, int nx, int ny, int nz, int pnx, int r,
               double out[4]);

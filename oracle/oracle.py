@@ -50,6 +50,7 @@ def lib():
         L.go_step.argtypes = [i, i, i, i, i, d, d, d, d, i]
         L.go_run.argtypes = [i, i, i, i, i, i, d, d, d, d, i]
         L.go_norms.argtypes = [d, d, i, i, i, i, i, d]
+        L.go_run_source.argtypes = [i, i, i, i, i, i, d, d, d, d, ctypes.POINTER(ctypes.c_int), d, i, i]
         L.go_seeded_value.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_double, ctypes.c_double]
         L.go_seeded_value.restype = ctypes.c_double
         L.go_default_coefs.argtypes = [d]
@@ -110,6 +111,17 @@ class Grid:
                          _p(self.U1), _p(self.U2), _p(self.U3), _p(self.coef), nthreads)
         if e:
             raise ValueError(f"oracle go_run error {e}")
+        return self
+
+    def run_source(self, nt, pt, source, nthreads=1):
+        """run() with source[it] added at array point pt = (i, j, k) after sweep it
+        (src/kernels/nb_naive_ts.c:190,196)."""
+        src = np.ascontiguousarray(source, dtype=np.float64)
+        p3 = (ctypes.c_int * 3)(*pt)
+        e = lib().go_run_source(self.op, self.nx, self.ny, self.nz, self.pnx, nt, _p(self.U1), _p(self.U2),
+                                _p(self.U3), _p(self.coef), p3, _p(src), len(src), nthreads)
+        if e:
+            raise ValueError(f"oracle go_run_source error {e}")
         return self
 
     def step(self, u, v, nthreads=1):

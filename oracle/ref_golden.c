@@ -14,7 +14,13 @@
  *   init = "seeded" : fields / roc2 / coefficient arrays overwritten with the
  *                     oracle's seeded values after the reference's allocation;
  *                     optional c0..c4 replace the constant coefficients.
- * Prints "ldomain <nnx> <nny> <nnz> nt <nt>" on stdout.
+ * With GIRIH_REF_SOURCE=1 in the environment the reference's source-point
+ * update runs (src/kernels/nb_naive_ts.c:190,196): the point is the
+ * reference's centred source (src/utils.c:247-251, 302-315) and the values are
+ * the reference's source[i] = i (src/performance.c:53-54).  The reference's
+ * init() switches the update off (src/utils.c:336); the harness switches it
+ * back on after init.
+ * Prints "ldomain <nnx> <nny> <nnz> nt <nt> source <i> <j> <k>" on stdout.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -33,6 +39,7 @@ extern void arrays_allocate(Parameters *);
 extern void arrays_free(Parameters *);
 extern void init_coeff(Parameters *);
 extern void domain_data_fill(Parameters *);
+extern void set_centered_source(Parameters *);
 extern void naive_nonblocking_ts(Parameters *);
 extern void halo_first_ts(Parameters *);
 extern void dynamic_intra_diamond_ts(Parameters *);
@@ -70,6 +77,7 @@ int main(int argc, char **argv) {
   p.stencil_ctx.thread_group_size = 2;
   p.orig_thread_group_size = 2;
 
+  set_centered_source(&p);
   mpi_topology_init(&p);
   init(&p);
   mpi_halo_init(&p);
@@ -97,6 +105,16 @@ int main(int argc, char **argv) {
     return 2;
   }
 
+  const char *src_env = getenv("GIRIH_REF_SOURCE");
+  const int with_source = src_env && atoi(src_env) == 1;
+  if (with_source) {
+    p.source_point_enabled = 1;
+    /* nt + 1 values: the stepper reads source[nt] after the extra sweep of an odd nt */
+    p.source = (real_t *)malloc(sizeof(real_t) * (size_t)(p.nt + 1));
+    if (!p.source) return 5;
+    for (int i = 0; i <= p.nt; i++) p.source[i] = i < p.nt ? (real_t)i : 0;
+  }
+
   TSList[p.target_ts].func(&p);
 
   FILE *f = fopen(out, "wb");
@@ -104,8 +122,9 @@ int main(int argc, char **argv) {
   fwrite(p.U1, sizeof(real_t), p.ln_domain, f);
   fwrite(p.U2, sizeof(real_t), p.ln_domain, f);
   fclose(f);
-  printf("ldomain %d %d %d nt %d\n", p.ldomain_shape[0], p.ldomain_shape[1], p.ldomain_shape[2],
-         p.nt);
+  printf("ldomain %d %d %d nt %d source %d %d %d\n", p.ldomain_shape[0], p.ldomain_shape[1],
+         p.ldomain_shape[2], p.nt, with_source ? p.lsource_pt[0] : -1, with_source ? p.lsource_pt[1] : -1,
+         with_source ? p.lsource_pt[2] : -1);
   arrays_free(&p);
   mpi_halo_finalize(&p);
   return 0;

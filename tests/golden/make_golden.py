@@ -48,9 +48,16 @@ CASES = [
     ("k5_ragged", 5, 7, 3, 5, 3, "seeded", dict(seed=31, f=(0, 1), roc2=(0, 0), c=(0.01, 0.1), coefs=None)),
     ("k7_seed", 7, 13, 11, 9, 4, "seeded", dict(seed=7, f=(0, 1), roc2=(0, 0), c=(0, 0), coefs=[-0.5, 0.05, 0.02, 0.01])),
 ]
+# with the reference's source-point update switched on (GIRIH_REF_SOURCE=1): the
+# reference's centred point and source[i] = i
+SOURCE_CASES = [
+    ("k1_src", 1, 13, 11, 9, 6, "ref", None),
+    ("k0_src", 0, 12, 10, 9, 6, "seeded", dict(seed=2, f=(-1, 1), roc2=(0.05, 0.15), c=(0, 0), coefs=LAP8)),
+    ("k5_src", 5, 13, 11, 9, 4, "seeded", dict(seed=3, f=(0, 1), roc2=(0, 0), c=(0.01, 0.1), coefs=None)),
+]
 
 
-def run_case(op, nx, ny, nz, nt, init, sp):
+def run_case(op, nx, ny, nz, nt, init, sp, source=False):
     with tempfile.TemporaryDirectory() as td:
         out = os.path.join(td, "g.bin")
         cmd = [HARNESS, str(op), str(nx), str(ny), str(nz), str(nt), "0", init, out]
@@ -58,25 +65,29 @@ def run_case(op, nx, ny, nz, nt, init, sp):
             cmd += [str(sp["seed"])] + [repr(float(x)) for x in (*sp["f"], *sp["roc2"], *sp["c"])]
             if sp.get("coefs"):
                 cmd += [repr(float(x)) for x in sp["coefs"]]
-        env = dict(os.environ, OMP_NUM_THREADS="2")
+        env = dict(os.environ, OMP_NUM_THREADS="2", GIRIH_REF_SOURCE="1" if source else "0")
         res = subprocess.run(cmd, check=True, capture_output=True, text=True, env=env)
         tok = res.stdout.split()
         nnx, nny, nnz = int(tok[1]), int(tok[2]), int(tok[3])
+        pt = [int(x) for x in tok[7:10]]
         raw = np.fromfile(out, dtype=np.float64)
         n = nnx * nny * nnz
         assert raw.size == 2 * n
-        return raw[:n].reshape(nnz, nny, nnx), raw[n:].reshape(nnz, nny, nnx)
+        return raw[:n].reshape(nnz, nny, nnx), raw[n:].reshape(nnz, nny, nnx), pt
 
 
 def main():
     if not os.path.exists(HARNESS):
         sys.exit("build the reference first: make -C oracle ref")
     arrays, specs = {}, {}
-    for name, op, nx, ny, nz, nt, init, sp in CASES:
-        u1, u2 = run_case(op, nx, ny, nz, nt, init, sp)
+    for (name, op, nx, ny, nz, nt, init, sp), source in ([(c, False) for c in CASES] +
+                                                          [(c, True) for c in SOURCE_CASES]):
+        u1, u2, pt = run_case(op, nx, ny, nz, nt, init, sp, source)
         arrays[name + "__U1"] = u1
         arrays[name + "__U2"] = u2
         specs[name] = dict(op=op, nx=nx, ny=ny, nz=nz, nt=nt, init=init, seeded=sp)
+        if source:
+            specs[name]["source_pt"] = pt  # (i, j, k) array indices; values source[i] = i
         print(f"{name}: ldomain {u1.shape[::-1]}")
     arrays["specs"] = np.frombuffer(json.dumps(specs).encode(), dtype=np.uint8)
     np.savez_compressed(os.path.join(HERE, "golden_ref.npz"), **arrays)

@@ -37,7 +37,10 @@ def _grid_for(name):
 def test_oracle_bit_exact_vs_reference(name, nthreads):
     g, s = _grid_for(name)
     assert g.U1.shape == _data[name + "__U1"].shape
-    g.run(s["nt"], nthreads=nthreads)
+    if "source_pt" in s:
+        g.run_source(s["nt"], s["source_pt"], np.arange(s["nt"], dtype=np.float64), nthreads=nthreads)
+    else:
+        g.run(s["nt"], nthreads=nthreads)
     np.testing.assert_array_equal(g.U1, _data[name + "__U1"])
     np.testing.assert_array_equal(g.U2, _data[name + "__U2"])
 
@@ -99,3 +102,21 @@ def test_seeded_values_are_deterministic_and_in_range():
     assert abs(np.mean(a) - 0.5) < 0.05
     c = [oracle.seeded_value(2, 0, i, 0.0, 1.0) for i in range(1000)]
     assert a != c
+
+
+def test_source_cases_differ_from_sourceless_runs():
+    """The source-point golden cases are not the plain run: the update was on."""
+    for name, s in SPECS.items():
+        if "source_pt" not in s:
+            continue
+        g, _ = _grid_for(name)
+        g.run(s["nt"])
+        assert not np.array_equal(g.U2, _data[name + "__U2"]), name
+        i, j, k = s["source_pt"]
+        assert g.r <= i < g.nx + g.r and g.r <= j < g.ny + g.r and g.r <= k < g.nz + g.r
+
+
+def test_oracle_source_rejects_halo_point():
+    g, s = _grid_for("k1_src")
+    with pytest.raises(ValueError):
+        g.run_source(2, (0, 5, 5), [1.0, 2.0])

@@ -23,6 +23,11 @@ struct girih_gpu_ctx {
   void *dfr2 = nullptr;
   void *coef = nullptr;
   float *scale = nullptr;
+  // source point: device element offset, value count, device values (FP64)
+  int64_t src_off = -1;
+  int src_n = 0;
+  double *d_src = nullptr;
+  int d_src_cap = 0;
   double cc[5] = {0, 0, 0, 0, 0};
   void *staging = nullptr;
   size_t staging_bytes = 0;

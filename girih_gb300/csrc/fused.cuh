@@ -40,6 +40,9 @@ struct FusedLaunch {
   const void *tma_cur, *tma_prev, *tma_roc2;  // host CUtensorMap objects (TMA variants)
   const void *coef;        // variable coefficients (device layout arrays)
   const float *cscale;     // per-array scales of BF16 coefficients (mixed form)
+  const double *src;       // source values per step (null: no source point)
+  int src_off;             // device element offset of the source point
+  int src_t0, src_n;       // step index of this pass's first level; number of values
 };
 
 bool fused_supported(const Geom &g, int precision);

@@ -42,6 +42,8 @@ template <class S> struct FusedArgs {
   unsigned *range_flag;  // error flags (bit 1: a TMA copy timed out)
   const void *coef;      // variable coefficients: nc arrays of g.elems (S, or BF16 in the mixed form)
   const float *cscale;   // per-array scales of BF16 coefficients
+  const double *src;     // source point values per step (null: none)
+  int src_off, src_t0, src_n;
 };
 
 // Storage type of a compute type (every compute type is stored as itself).
@@ -272,6 +274,18 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
     else coeff = CoefFull<T>{static_cast<const T *>(a.coef), g.elems};
   }
 
+  // source point: its plane, and per row the position inside this thread's
+  // x group (-1: not this thread's)
+  int src_z = -(1 << 30), src_v[CY];
+#pragma unroll
+  for (int c = 0; c < CY; c++) src_v[c] = -1;
+  if (a.src != nullptr) {
+    src_z = a.src_off / plane;
+    const int xy = a.src_off - src_z * plane;
+#pragma unroll
+    for (int c = 0; c < CY; c++) src_v[c] = (xy - col[c] >= 0 && xy - col[c] < VX) ? xy - col[c] : -1;
+  }
+
   T q[TT][CY][VX][QL];
 #pragma unroll
   for (int l = 0; l < TT; l++)
@@ -456,6 +470,21 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
             else val[V] = on ? cand : centre;  // halo and out-of-region points keep their value
           });
           }
+          // source point of step src_t0 + L - 1, added after the update's rounding
+          // (every tile holding the point adds it, so overlapping halos agree)
+          if (p == src_z && src_v[c] >= 0) {
+            const int st = a.src_t0 + L - 1;
+            if (st < a.src_n) {
+              const T sv = coef_to_compute<T>(a.src[st]);
+              static_for<VX>([&](auto v_c) {
+                constexpr int V = decltype(v_c)::value;
+                if (V == src_v[c]) {
+                  if constexpr (std::is_same<T, Df64>::value) val[V] = df_norm(val[V] + sv);
+                  else val[V] = val[V] + sv;
+                }
+              });
+            }
+          }
           if constexpr (L == TT || L == TT - 1) {
             if (p_out && y_outr[c] && (L == TT || a.write_prev)) {
               ST *dst = (L == TT ? a.out_cur : a.out_prev) + poff + col[c];
@@ -596,6 +625,10 @@ cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
   a.range_flag = L.range_flag;
   a.coef = L.coef;
   a.cscale = L.cscale;
+  a.src = L.src;
+  a.src_off = L.src_off;
+  a.src_t0 = L.src_t0;
+  a.src_n = L.src_n;
   a.zchunk = zchunk;
   a.write_prev = L.write_prev;
   if constexpr (TMA) {

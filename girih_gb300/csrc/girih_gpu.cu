@@ -309,8 +309,20 @@ int issue_steps_impl(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *
       for (int h = 0; h < 2; h++) {
         void *u = c->f[h == 0 ? *iu1 : *iu2];
         const void *v = c->f[h == 0 ? *iu2 : *iu1];
-        cudaError_t e = c->tsz == 8 ? launch_plain<double>(step_args<double>(c, u, v), exact, false, st)
-                                    : launch_plain<float>(step_args<float>(c, u, v), exact, c->bf16coef, st);
+        const int sweep = s + h;
+        const double *src = c->d_src && sweep < c->src_n ? c->d_src + sweep : nullptr;
+        cudaError_t e;
+        if (c->tsz == 8) {
+          StepArgs<double> a = step_args<double>(c, u, v);
+          a.src = src;
+          a.src_off = c->src_off;
+          e = launch_plain<double>(a, exact, false, st);
+        } else {
+          StepArgs<float> a = step_args<float>(c, u, v);
+          a.src = src;
+          a.src_off = c->src_off;
+          e = launch_plain<float>(a, exact, c->bf16coef, st);
+        }
         if (e != cudaSuccess) return fail(GIRIH_GPU_ECUDA, std::string("plain launch: ") + cudaGetErrorString(e));
         (*launches)++;
       }
@@ -355,6 +367,12 @@ int issue_steps_impl(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *
     L.range_flag = flag;
     L.coef = c->coef;
     L.cscale = c->scale;
+    if (c->d_src && c->src_n > 0) {
+      L.src = c->d_src;
+      L.src_off = (int)c->src_off;
+      L.src_t0 = steps - left;
+      L.src_n = c->src_n;
+    }
     if (c->fcfg.box_w > 0) {  // TMA variant
       L.tma_prev = tensor_map(c, *iu1, c->f[*iu1]);
       L.tma_cur = tensor_map(c, *iu2, c->f[*iu2]);
@@ -514,6 +532,7 @@ void girih_gpu_destroy(girih_gpu_ctx *c) {
   for (void *p : c->dfp)
     if (p) cudaFree(p);
   if (c->dfr2) cudaFree(c->dfr2);
+  if (c->d_src) cudaFree(c->d_src);
   if (c->roc2) cudaFree(c->roc2);
   if (c->coef) cudaFree(c->coef);
   if (c->scale) cudaFree(c->scale);
@@ -842,6 +861,39 @@ int girih_gpu_autotune(girih_gpu_ctx *c, int trial_steps, girih_gpu_info_t *chos
     g_tune_cache[std::make_tuple(g.op, prec, size_class(g))] = best_c;
   }
   return girih_gpu_info(c, chosen);
+}
+
+int girih_gpu_set_source(girih_gpu_ctx *c, const int pt[3], const double *source, int n) {
+  if (!c) return fail(GIRIH_GPU_EINVAL, "null context");
+  if (n < 0) return fail(GIRIH_GPU_EINVAL, "negative source count");
+  DeviceGuard dg(c->d.device);
+  drop_graph(c);  // the captured launches carry the source arguments
+  if (!source || n == 0) {
+    c->src_n = 0;
+    c->src_off = -1;
+    return 0;
+  }
+  if (!pt) return fail(GIRIH_GPU_EINVAL, "null source point");
+  const Geom &g = c->g;
+  const int n3[3] = {g.nx, g.ny, g.nz};
+  for (int a = 0; a < 3; a++)
+    if (pt[a] < g.r || pt[a] >= n3[a] + g.r) return fail(GIRIH_GPU_EINVAL, "source point outside the interior");
+  if (n > c->d_src_cap) {
+    if (c->d_src) {
+      cudaFree(c->d_src);
+      c->dev_bytes -= 8.0 * c->d_src_cap;
+      c->d_src = nullptr;
+      c->d_src_cap = 0;
+    }
+    int e = dev_alloc(c, (void **)&c->d_src, (size_t)n * sizeof(double));
+    if (e) return e;
+    c->d_src_cap = n;
+  }
+  CK(cudaMemcpyAsync(c->d_src, source, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->src_off = g.at(pt[0], pt[1], pt[2]);  // array indices include the halo
+  c->src_n = n;
+  return 0;
 }
 
 int girih_gpu_info(girih_gpu_ctx *c, girih_gpu_info_t *info) {

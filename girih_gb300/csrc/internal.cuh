@@ -40,6 +40,8 @@ template <class T> struct StepArgs {
   const void *coef;   // variable coefficients (T or bf16)
   const float *scale; // bf16 per-array scales (mixed precision)
   T cc[5];            // constant coefficients
+  const double *src;  // source point: value of this sweep at src[0] (null: no update)
+  int64_t src_off;    // device element offset of the source point
 };
 
 // Plain (one step per launch) kernels: plain.cu

@@ -54,7 +54,10 @@ __global__ void __launch_bounds__(kBX *kBY) plain_step(StepArgs<T> a, Cf coef, i
       uold = a.u[c];
       r2 = __ldg(a.roc2 + c);
     }
-    a.u[c] = apply_op<OP, A>(cc, coef, c, acc, uold, r2);
+    T val = apply_op<OP, A>(cc, coef, c, acc, uold, r2);
+    // source point: added after the sweep's own rounding (nb_naive_ts.c:190)
+    if (a.src != nullptr && c == a.src_off) val = A::add(val, (T)a.src[0]);
+    a.u[c] = val;
 #pragma unroll
     for (int d = 0; d < 2 * R; d++) q[d] = q[d + 1];
   }

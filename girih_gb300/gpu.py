@@ -73,6 +73,7 @@ def lib():
         L.girih_gpu_fill_seeded.argtypes = [P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double),
                                             ctypes.POINTER(ctypes.c_double), ctypes.c_int]
         L.girih_gpu_download_roc2.argtypes = [P, P]
+        L.girih_gpu_set_source.argtypes = [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double), ctypes.c_int]
         L.girih_gpu_fused_run_noalloc.argtypes = [ctypes.POINTER(Desc), P, P, P, ctypes.POINTER(ctypes.c_double),
                                                   ctypes.c_int, P]
         L.girih_gpu_info.argtypes = [P, ctypes.POINTER(Info)]
@@ -171,6 +172,17 @@ class Context:
         if coefs is not None:
             cc = (ctypes.c_double * 5)(*(list(coefs)[:5] + [0.0] * (5 - len(coefs[:5]))))
         _check(lib().girih_gpu_fill_seeded(self._h, seed, rng, cc, 1 if f32_exact else 0), "girih_gpu_fill_seeded")
+
+    def set_source(self, pt, values):
+        """Source-point update of later runs: after sweep s, values[s] is added at
+        array point pt = (i, j, k) (halo included).  values=None switches it off."""
+        if values is None or len(values) == 0:
+            _check(lib().girih_gpu_set_source(self._h, None, None, 0), "girih_gpu_set_source")
+            return
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        p3 = (ctypes.c_int * 3)(*pt)
+        _check(lib().girih_gpu_set_source(self._h, p3, v.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), len(v)),
+               "girih_gpu_set_source")
 
     def download_roc2(self, U3=None):
         if U3 is None:

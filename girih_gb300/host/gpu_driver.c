@@ -6,7 +6,8 @@
  * --verify/...), topology, initialisation, then verification or the
  * performance test.  The only difference is the table below, which the
  * reference defines in src/wrappers.h:28-36: entry 3 is the GPU stepper, so
- * `--target-ts 3` runs the hot path on the GPU and `--list` shows it.
+ * `--target-ts 3` runs the hot path on the GPU and `--list` shows it; after a
+ * GPU performance run the rates are also printed in scripts/parse.py's keys.
  */
 #include <stdio.h>
 
@@ -16,6 +17,7 @@ extern void naive_nonblocking_ts(Parameters *p);
 extern void halo_first_ts(Parameters *p);
 extern void dynamic_intra_diamond_ts(Parameters *p);
 extern void gpu_ts(Parameters *p);
+extern void gpu_ts_report(const Parameters *p);
 
 extern void param_default(Parameters *);
 extern void parse_args(int argc, char **argv, Parameters *);
@@ -52,10 +54,12 @@ int main(int argc, char **argv) {
   }
   mpi_topology_init(&p);
   init(&p);
-  if (p.verify != 0)
+  if (p.verify != 0) {
     verify(&p);
-  else
+  } else {
     performance_test(&p);
+    if (TSList[p.target_ts].func == gpu_ts) gpu_ts_report(&p);  /* scripts/parse.py keys */
+  }
   MPI_Finalize();
   return 0;
 }

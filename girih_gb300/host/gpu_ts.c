@@ -19,16 +19,35 @@
  *                         so --verify 1 passes its bit-exact check) | 0
  *   GIRIH_GPU_DEVICE    = CUDA device ordinal (default 0)
  * Errors are reported through the reference's RAISE_ERROR.
+ *
+ * gpu_ts_report() prints the run's rates in the key format of the reference's
+ * scripts/parse.py (get_summary: "RANK0 MStencil/s  MIN/AVG/MAX"), which the
+ * reference's own report no longer emits (it prints GStencil/s,
+ * src/utils.c:872-875), so the existing plotting scripts ingest GPU runs.
  */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #include "data_structures.h"
 #include "girih_gpu.h"
 
 static girih_gpu_ctx *g_ctx = NULL;
 static girih_gpu_desc g_desc;
+
+/* per-call wall time (the span the reference's MPI_Wtime bracket measures,
+ * src/performance.c:74-78) and device time, over all calls */
+static struct {
+  int calls;
+  double wall_min, wall_max, wall_sum, dev_min;
+} g_stats;
+
+static double wall_now(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
 
 static int env_choice(const char *name, const char *const *names, int n, int def) {
   const char *v = getenv(name);
@@ -52,6 +71,7 @@ static void gpu_ts_fail(Parameters *p, const char *what, int err) {
 }
 
 void gpu_ts(Parameters *p) {
+  const double t0 = wall_now();
   static const char *const precisions[] = {"fp64", "fp32", "mixed"};
   static const char *const schedules[] = {"plain", "fused", "auto"};
   if (p->mpi_size != 1) RAISE_ERROR("the GPU time stepper runs one grid per process: use a single rank");
@@ -84,6 +104,17 @@ void gpu_ts(Parameters *p) {
     atexit(gpu_ts_release);
   }
   if ((e = girih_gpu_upload(g_ctx, p->U1, p->U2, p->U3, p->coef))) gpu_ts_fail(p, "girih_gpu_upload", e);
+  /* the reference's source-point update (nb_naive_ts.c:190,196), when switched on */
+  if (p->source_point_enabled == 1 && p->has_source == 1 && p->source && p->nt > 0) {
+    double *src = (double *)malloc(sizeof(double) * (size_t)p->nt);
+    if (!src) RAISE_ERROR("host allocation failed");
+    for (int i = 0; i < p->nt; i++) src[i] = (double)p->source[i];
+    e = girih_gpu_set_source(g_ctx, p->lsource_pt, src, p->nt);
+    free(src);
+    if (e) gpu_ts_fail(p, "girih_gpu_set_source", e);
+  } else if ((e = girih_gpu_set_source(g_ctx, NULL, NULL, 0))) {
+    gpu_ts_fail(p, "girih_gpu_set_source", e);
+  }
   float ms = 0.f;
   if ((e = girih_gpu_run(g_ctx, p->nt, &ms))) gpu_ts_fail(p, "girih_gpu_run", e);
   if ((e = girih_gpu_download(g_ctx, p->U1, p->U2))) gpu_ts_fail(p, "girih_gpu_download", e);
@@ -91,6 +122,12 @@ void gpu_ts(Parameters *p) {
   /* the device time of the loop is the stepper's compute time
    * (the reference accumulates it the same way, nb_naive_ts.c:205-206) */
   p->prof.compute += ms * 1e-3;
+  const double wall = wall_now() - t0;
+  if (g_stats.calls == 0 || wall < g_stats.wall_min) g_stats.wall_min = wall;
+  if (g_stats.calls == 0 || wall > g_stats.wall_max) g_stats.wall_max = wall;
+  if (g_stats.calls == 0 || ms * 1e-3 < g_stats.dev_min) g_stats.dev_min = ms * 1e-3;
+  g_stats.wall_sum += wall;
+  g_stats.calls++;
   if (p->verbose && p->mpi_rank == 0) {
     girih_gpu_info_t info;
     girih_gpu_info(g_ctx, &info);
@@ -99,4 +136,16 @@ void gpu_ts(Parameters *p) {
            precisions[info.precision], schedules[info.schedule], info.fusion_depth, info.launches_last_run, ms,
            ms > 0 ? (double)p->ln_stencils * steps / (ms * 1e6) : 0.0);
   }
+}
+
+/* Rates of the calls so far in scripts/parse.py's keys (MStencil/s per time
+ * step: ln_stencils * nt / time, the reference's GStencil/s x 1000), plus the
+ * device-only rate of the fastest call. */
+void gpu_ts_report(const Parameters *p) {
+  if (p->mpi_rank != 0 || g_stats.calls == 0) return;
+  const double per_step = (double)p->ln_stencils * p->nt / 1e6;
+  printf("RANK0 MStencil/s  MIN: %f\n", per_step / g_stats.wall_max);
+  printf("RANK0 MStencil/s  AVG: %f\n", per_step / (g_stats.wall_sum / g_stats.calls));
+  printf("RANK0 MStencil/s  MAX: %f\n", per_step / g_stats.wall_min);
+  if (g_stats.dev_min > 0) printf("GPU device MStencil/s MAX: %f\n", per_step / g_stats.dev_min);
 }

@@ -146,6 +146,17 @@ int girih_gpu_fill_seeded(girih_gpu_ctx *c, uint64_t seed, const double ranges[6
  * the caller's array in the reference layout. */
 int girih_gpu_download_roc2(girih_gpu_ctx *c, void *U3);
 
+/* Source-point injection, the reference's per-sweep point update
+ * (src/kernels/nb_naive_ts.c:190,196: U(lsource_pt) += source[it]): in every
+ * later girih_gpu_run, after sweep s (counted from 0 within the run) the array
+ * just updated gets source[s] added at the array point pt = {i, j, k} (indices
+ * with the halo, as the reference's lsource_pt, src/utils.c:310).  Sweeps
+ * s >= n add nothing; n = 0 or source = NULL switches the update off.  pt must
+ * be an interior point (GIRIH_GPU_EINVAL otherwise).  The n values are copied.
+ * Every schedule and precision applies it; the value is added in the compute
+ * precision after the sweep's own rounding, as the reference does. */
+int girih_gpu_set_source(girih_gpu_ctx *c, const int pt[3], const double *source, int n);
+
 int girih_gpu_info(girih_gpu_ctx *c, girih_gpu_info_t *info);
 
 /* Autotuner (replaces the reference's CPU tile auto-tuning, auto_tune_params in

@@ -45,3 +45,59 @@ def test_gpu_stepper_without_gpu_reports_error():
                         "--target-ts", "3", "--verify", "1"], capture_output=True, text=True)
     assert r.returncode == 1
     assert "no usable CUDA device" in r.stderr
+
+
+@pytest.fixture(scope="module")
+def oracle_stub(tmp_path_factory, driver):
+    """libgirih_gpu.so stand-in backed by the CPU oracle (tests/c/oracle_gpu_stub.c),
+    loaded ahead of the real library through LD_LIBRARY_PATH (the driver's
+    search path is a RUNPATH)."""
+    d = tmp_path_factory.mktemp("stub")
+    subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+                    "-I", os.path.join(ROOT, "include"), "-I", os.path.join(ROOT, "oracle"),
+                    os.path.join(ROOT, "tests", "c", "oracle_gpu_stub.c"), os.path.join(ROOT, "oracle", "girih_oracle.c"),
+                    "-o", str(d / "libgirih_gpu.so"), "-lm"], check=True)
+    return dict(os.environ, LD_LIBRARY_PATH=str(d), OMP_NUM_THREADS="2")
+
+
+@pytest.mark.parametrize("kernel", ["1", "0", "5"])
+def test_gpu_stepper_host_logic_verifies(driver, oracle_stub, kernel):
+    """gpu_ts.c end to end (shapes, upload, run, download) against the
+    reference's own --verify 1 bit-exact check, the device replaced by the oracle."""
+    r = subprocess.run([driver, "--nx", "20", "--ny", "14", "--nz", "12", "--nt", "6", "--target-kernel", kernel,
+                        "--target-ts", "3", "--verify", "1"], capture_output=True, text=True, env=oracle_stub)
+    assert r.returncode == 0, r.stderr
+    assert "PASSED" in r.stdout
+
+
+def _parse_py_summary(text):
+    """The key matching of the reference's scripts/parse.py get_summary():
+    a line starting with '<field>:' gives the first token after the colon."""
+    import re
+    floats = ("RANK0 MStencil/s  MIN", "RANK0 MStencil/s  AVG", "RANK0 MStencil/s  MAX", "RANK0 Total",
+              "RANK0 Computation")
+    strs = ("Time stepper name", "Stencil Kernel name", "Stencil Kernel coefficients", "Precision")
+    ints = ("Number of time steps", "Number of tests", "OpenMP Threads", "MPI size")
+    out = {}
+    for line in text.splitlines():
+        for f in floats:
+            if re.match("^" + re.escape(f) + ":", line):
+                out[f] = float(line.split(":")[1].split()[0])
+        for f in ints:
+            if re.match("^" + re.escape(f) + ":", line):
+                out[f] = int(line.split(":")[1].split()[0])
+        for f in strs:
+            if re.match("^" + re.escape(f) + ":", line):
+                out[f] = line.split(":")[1].strip()
+    return out
+
+
+def test_gpu_stepper_report_has_parse_py_keys(driver, oracle_stub):
+    r = subprocess.run([driver, "--nx", "24", "--ny", "24", "--nz", "24", "--nt", "4", "--target-kernel", "1",
+                        "--target-ts", "3", "--n-tests", "3"], capture_output=True, text=True, env=oracle_stub)
+    assert r.returncode == 0, r.stderr
+    m = _parse_py_summary(r.stdout)
+    assert m["Time stepper name"] == "GPU (libgirih_gpu)"
+    assert m["Number of time steps"] == 4 and m["Number of tests"] == 3
+    assert 0 < m["RANK0 MStencil/s  MIN"] <= m["RANK0 MStencil/s  AVG"] * 1.0001 <= m["RANK0 MStencil/s  MAX"] * 1.0002
+    assert "GPU device MStencil/s MAX:" in r.stdout

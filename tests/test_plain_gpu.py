@@ -38,10 +38,18 @@ def _golden_grid(name):
     return g, s
 
 
+def _set_golden_source(ctx, s):
+    """Golden cases run with the reference's source update carry its point; the
+    values are the reference's source[i] = i."""
+    if "source_pt" in s:
+        ctx.set_source(s["source_pt"], np.arange(s["nt"], dtype=np.float64))
+
+
 @pytest.mark.parametrize("name", GPU_CASES)
 def test_exact_fp64_is_bit_identical_to_reference(name):
     g, s = _golden_grid(name)
     with gpu_context(g, precision="fp64", schedule="plain", exact=True) as ctx:
+        _set_golden_source(ctx, s)
         ctx.run(s["nt"])
         u1, u2 = ctx.download()
     np.testing.assert_array_equal(g.interior(u1), g.interior(_data[name + "__U1"]))
@@ -53,6 +61,7 @@ def test_exact_fp64_is_bit_identical_to_reference(name):
 def test_fast_fp64_within_1e12(name):
     g, s = _golden_grid(name)
     with gpu_context(g, precision="fp64", schedule="plain") as ctx:
+        _set_golden_source(ctx, s)
         ctx.run(s["nt"])
         u1, u2 = ctx.download()
         dev = gpu.rel_errors(ctx.error_norms(_data[name + "__U1"]))[0]

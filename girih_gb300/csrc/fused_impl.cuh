@@ -195,7 +195,7 @@ struct FusedShape {
 // One CTA-tile of a fused pass: tile (bxi, byi) of the x-y tiling, z chunk bzi,
 // executed by the NTX*NTY threads of the calling CTA (thread (tx, ty)).  Used by
 // the single-grid kernel below and by the batched persistent kernel.
-template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX, bool TMA = false>
+template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX, bool TMA = false, bool SRC = false>
 __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>::type> &a, int bxi, int byi,
                                            int bzi, int tx, int ty, unsigned char *smraw,
                                            const TmaMaps *maps = nullptr) {
@@ -279,7 +279,7 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
   int src_z = -(1 << 30), src_v[CY];
 #pragma unroll
   for (int c = 0; c < CY; c++) src_v[c] = -1;
-  if (a.src != nullptr) {
+  if (SRC && a.src != nullptr) {
     src_z = a.src_off / plane;
     const int xy = a.src_off - src_z * plane;
 #pragma unroll
@@ -472,7 +472,7 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
           }
           // source point of step src_t0 + L - 1, added after the update's rounding
           // (every tile holding the point adds it, so overlapping halos agree)
-          if (p == src_z && src_v[c] >= 0) {
+          if (SRC && p == src_z && src_v[c] >= 0) {
             const int st = a.src_t0 + L - 1;
             if (st < a.src_n) {
               const T sv = coef_to_compute<T>(a.src[st]);
@@ -554,11 +554,11 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
   }
 }
 
-template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX>
+template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX, bool SRC = false>
 __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<typename StorageOf<T>::type> a) {
   extern __shared__ __align__(128) unsigned char smraw[];
-  fused_tile<OP, T, COMP, TT, NTX, NTY, CY, VX>(a, blockIdx.x, blockIdx.y, blockIdx.z, threadIdx.x, threadIdx.y,
-                                                smraw);
+  fused_tile<OP, T, COMP, TT, NTX, NTY, CY, VX, false, SRC>(a, blockIdx.x, blockIdx.y, blockIdx.z, threadIdx.x,
+                                                            threadIdx.y, smraw);
 }
 
 // The same pass with the input planes staged by TMA; the tensor maps travel as
@@ -571,13 +571,13 @@ __global__ void __launch_bounds__(NTX *NTY)
                                                       threadIdx.y, smraw, &maps);
 }
 
-template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX, bool TMA>
+template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX, bool TMA, bool SRC = false>
 cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
   using S = FusedShape<OP, T, COMP, TT, NTX, NTY, CY, VX, TMA>;
   constexpr int R = S::R, BX = S::BX, BY = S::BY;
   void *kern;
   if constexpr (TMA) kern = (void *)fused_pass_tma<OP, T, COMP, TT, NTX, NTY, CY, VX>;
-  else kern = (void *)fused_pass<OP, T, COMP, TT, NTX, NTY, CY, VX>;
+  else kern = (void *)fused_pass<OP, T, COMP, TT, NTX, NTY, CY, VX, SRC>;
   const size_t smem = S::smem_bytes;
   static bool attr_set = false;  // per instantiation, host side
   if (!attr_set) {
@@ -639,18 +639,18 @@ cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
     maps.roc2 = *static_cast<const CUtensorMap *>(L.tma_roc2);
     fused_pass_tma<OP, T, COMP, TT, NTX, NTY, CY, VX><<<dim3(gx, gy, nz_ch), dim3(NTX, NTY), smem, s>>>(a, maps);
   } else {
-    fused_pass<OP, T, COMP, TT, NTX, NTY, CY, VX><<<dim3(gx, gy, nz_ch), dim3(NTX, NTY), smem, s>>>(a);
+    fused_pass<OP, T, COMP, TT, NTX, NTY, CY, VX, SRC><<<dim3(gx, gy, nz_ch), dim3(NTX, NTY), smem, s>>>(a);
   }
   return cudaGetLastError();
 }
 
-template <int OP, class T, bool COMP, int NTX, int NTY, int CY, int VX, int TMAX, bool TMA = false>
+template <int OP, class T, bool COMP, int NTX, int NTY, int CY, int VX, int TMAX, bool TMA = false, bool SRC = false>
 cudaError_t launch_variant(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
   switch (L.steps) {
-    case 1: return launch_tt<OP, T, COMP, 1, NTX, NTY, CY, VX, TMA>(g, L, s);
-    case 2: if constexpr (TMAX >= 2) return launch_tt<OP, T, COMP, 2, NTX, NTY, CY, VX, TMA>(g, L, s); break;
-    case 3: if constexpr (TMAX >= 3) return launch_tt<OP, T, COMP, 3, NTX, NTY, CY, VX, TMA>(g, L, s); break;
-    case 4: if constexpr (TMAX >= 4) return launch_tt<OP, T, COMP, 4, NTX, NTY, CY, VX, TMA>(g, L, s); break;
+    case 1: return launch_tt<OP, T, COMP, 1, NTX, NTY, CY, VX, TMA, SRC>(g, L, s);
+    case 2: if constexpr (TMAX >= 2) return launch_tt<OP, T, COMP, 2, NTX, NTY, CY, VX, TMA, SRC>(g, L, s); break;
+    case 3: if constexpr (TMAX >= 3) return launch_tt<OP, T, COMP, 3, NTX, NTY, CY, VX, TMA, SRC>(g, L, s); break;
+    case 4: if constexpr (TMAX >= 4) return launch_tt<OP, T, COMP, 4, NTX, NTY, CY, VX, TMA, SRC>(g, L, s); break;
   }
   return cudaErrorInvalidValue;
 }
@@ -669,6 +669,15 @@ cudaError_t launch_fused_op_impl(const Geom &g, const FusedConfig &cfg, const Fu
   // TMA variants (2, 3) are built for FP32 storage, where the rings fit shared
   // memory, and for the constant-coefficient operators
   constexpr bool kTma = std::is_same<T, float>::value && !OpTraits<OP>::VAR;
+  // with a source point every pass runs the source-enabled build of the first
+  // tile variant (the update is compiled out of the others); the kernel
+  // derives its tiling from its own shape
+  if (L.src != nullptr) {
+    if constexpr (std::is_same<T, Df64>::value || OpTraits<OP>::R != 1)
+      return launch_variant<OP, T, COMP, 64, 16, 2, 1, TM, false, true>(g, L, s);
+    else
+      return launch_variant<OP, T, COMP, 32, 16, 2, 2, TM, false, true>(g, L, s);
+  }
   if constexpr (std::is_same<T, Df64>::value) {  // one column per thread: pairs already fill 8 bytes
     switch (cfg.variant) {
       case 0: return launch_variant<OP, T, COMP, 64, 16, 2, 1, TM>(g, L, s);  // 64 x 32 region, 1024 threads

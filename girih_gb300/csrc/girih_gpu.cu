@@ -324,7 +324,7 @@ int issue_steps_impl(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *
           e = launch_plain<float>(a, exact, c->bf16coef, st);
         }
         if (e != cudaSuccess) return fail(GIRIH_GPU_ECUDA, std::string("plain launch: ") + cudaGetErrorString(e));
-        (*launches)++;
+        *launches += src ? 2 : 1;  // the sweep, and the source-point update
       }
     }
     return 0;

@@ -54,10 +54,7 @@ __global__ void __launch_bounds__(kBX *kBY) plain_step(StepArgs<T> a, Cf coef, i
       uold = a.u[c];
       r2 = __ldg(a.roc2 + c);
     }
-    T val = apply_op<OP, A>(cc, coef, c, acc, uold, r2);
-    // source point: added after the sweep's own rounding (nb_naive_ts.c:190)
-    if (a.src != nullptr && c == a.src_off) val = A::add(val, (T)a.src[0]);
-    a.u[c] = val;
+    a.u[c] = apply_op<OP, A>(cc, coef, c, acc, uold, r2);
 #pragma unroll
     for (int d = 0; d < 2 * R; d++) q[d] = q[d + 1];
   }
@@ -100,7 +97,25 @@ cudaError_t dispatch(const StepArgs<T> &a, bool exact, bool bf16coef, cudaStream
 }  // namespace
 
 template <class T>
+cudaError_t launch_plain_sweep(const StepArgs<T> &a, bool exact, bool bf16coef, cudaStream_t s);
+
+// Source point of one sweep, after the sweep (nb_naive_ts.c:190,196): one
+// thread adds the value in the arithmetic of the sweep.
+template <class A, class T> __global__ void add_source(T *u, int64_t off, const double *src) {
+  u[off] = A::add(u[off], (T)src[0]);
+}
+
+template <class T>
 cudaError_t launch_plain(const StepArgs<T> &a, bool exact, bool bf16coef, cudaStream_t s) {
+  cudaError_t e = launch_plain_sweep(a, exact, bf16coef, s);
+  if (e != cudaSuccess || a.src == nullptr) return e;
+  if (exact) add_source<ExactArith, T><<<1, 1, 0, s>>>(a.u, a.src_off, a.src);
+  else add_source<FastArith, T><<<1, 1, 0, s>>>(a.u, a.src_off, a.src);
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_plain_sweep(const StepArgs<T> &a, bool exact, bool bf16coef, cudaStream_t s) {
   switch (a.g.op) {
     case 0: return dispatch<0>(a, exact, bf16coef, s);
     case 1: return dispatch<1>(a, exact, bf16coef, s);

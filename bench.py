@@ -37,7 +37,7 @@ WORKLOADS = {
     "star7_leapfrog_512": dict(op=8, n=512, nt=500, seed=1, f=(0.0, 1.0), roc2=(0.5, 1.5), coefs=[-0.75, 0.125]),
     "star7_jacobi_512": dict(op=1, n=512, nt=500, seed=1, f=(0.0, 1.0), roc2=(0.0, 0.0), coefs=[-0.28472, 0.16]),
     "star25_leapfrog_480": dict(op=0, n=480, nt=200, seed=2, f=(-1.0, 1.0), roc2=(0.05, 0.15),
-                                coefs=[-8.541667, 1.6, -0.2, 0.025396826, -0.0017857143]),
+                                coefs=[-8.541667, 1.6, -0.2, 0.025396826, -0.0017857143], error_nts=[50, 100]),
     # variable coefficients, coefficient arrays U(0.01, 0.1/radius)
     "var7_384": dict(op=5, n=384, nt=200, seed=3, f=(0.0, 1.0), roc2=(0.0, 0.0), c=(0.01, 0.1), coefs=None),
     "var25_384": dict(op=4, n=384, nt=200, seed=3, f=(0.0, 1.0), roc2=(0.0, 0.0), c=(0.01, 0.025), coefs=None),
@@ -210,18 +210,30 @@ def run_ours(args, wl, rank, world, local):
     # errors: fresh nt-step runs from the same init against the FP64 plain form
     errors = {}
     if "plain64" in forms and not args.no_error:
+        # checkpoints (cumulative steps; the last is nt): runs continue from the state
+        marks = [m for m in wl.get("error_nts", []) if 0 < m < nt] + [nt]
         ref = gpu.Context(op, n, n, n, device=local, precision="fp64", schedule="plain")
         ref.fill_seeded(wl["seed"], wl["f"], wl["roc2"], crange, coefs=wl["coefs"], f32_exact=True)
-        ref.run(nt)
+        others = {}
         for name, kw in forms.items():
             if name == "plain64":
                 continue
             c = gpu.Context(op, n, n, n, device=local, fusion_depth=args.depth if kw["schedule"] == "fused" else 0, **kw)
             # creation picks up the autotuned choice cached above for this operator and size
             c.fill_seeded(wl["seed"], wl["f"], wl["roc2"], crange, coefs=wl["coefs"], f32_exact=True)
-            c.run(nt)
-            mr, l2 = gpu.rel_errors(c.compare(ref))
-            errors[name] = {"max_rel": mr, "l2_rel": l2, "nt": nt, "against": "plain64 (FP64, parity-checked vs the oracle)"}
+            others[name] = c
+            errors[name] = {"nt": nt, "against": "plain64 (FP64, parity-checked vs the oracle)"}
+        done = 0
+        for m in marks:
+            ref.run(m - done)
+            for name, c in others.items():
+                c.run(m - done)
+                mr, l2 = gpu.rel_errors(c.compare(ref))
+                errors[name]["max_rel"], errors[name]["l2_rel"] = mr, l2
+                if len(marks) > 1:
+                    errors[name].setdefault("by_nt", {})[str(m)] = {"max_rel": mr, "l2_rel": l2}
+            done = m
+        for c in others.values():
             c.close()
         ref.close()
 

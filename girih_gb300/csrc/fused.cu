@@ -26,7 +26,8 @@ int fused_max_depth(const Geom &g, int precision) {
 //   each), variant 1 = 32 x 64 (16x64 threads, 1 row each);
 //   radius 4 (one column per thread): variant 0 = 64 x 32 (64x16 threads, 2
 //   rows), variant 1 = 32 x 64 (32x32 threads, 2 rows);
-//   variants 2 and 3: 0 and 1 with TMA-staged input planes;
+//   variants 2 and 3: 0 and 1 with TMA-staged input planes (variant 2 at
+//   depth 4: x quads, 16x32 threads, one row each);
 //   double-float: one column per thread in variants 0 = 64 x 32 (64x16 threads,
 //   2 rows), 1 = 32 x 32 (32x16 threads, 2 rows), 2 = 64 x 16 (64x16 threads,
 //   1 row); x pairs (radius 1) in variants 3 = 64 x 32 (32x16 threads, 2 rows)
@@ -51,6 +52,7 @@ FusedConfig make_fused_config(const Geom &g, int precision, int depth, int varia
     return c;
   int ntx, ry, vx;
   variant_shape(variant, g.r, precision, &ntx, &ry, &vx);
+  if (variant == 2 && g.r == 1 && depth == 4 && precision != GIRIH_FP64_DF) vx = 4;  // x quads at depth 4
   // double-buffered shared memory of all levels (rows padded by r), plus the TMA
   // rings of the TMA variants, must fit one CTA (227 KiB)
   const size_t tsz = (precision == GIRIH_FP64 || precision == GIRIH_FP64_DF) ? 8 : 4;

@@ -696,7 +696,12 @@ cudaError_t launch_fused_op_impl(const Geom &g, const FusedConfig &cfg, const Fu
     switch (cfg.variant) {
       case 0: return launch_variant<OP, T, COMP, 32, 16, 2, 2, TM>(g, L, s);  // 64 x 32 region, 512 threads
       case 1: return launch_variant<OP, T, COMP, 16, 64, 1, 2, TM>(g, L, s);  // 32 x 64 region, 1024 threads
-      case 2: if constexpr (kTma) return launch_variant<OP, T, COMP, 32, 16, 2, 2, TM, true>(g, L, s); break;
+      case 2:  // 64 x 32 region, 512 threads: x quads at depth 4, x pairs below (same tile: 4-column alignment)
+        if constexpr (kTma) {
+          if (L.steps == 4) return launch_tt<OP, T, COMP, 4, 16, 32, 1, 4, true>(g, L, s);
+          return launch_variant<OP, T, COMP, 32, 16, 2, 2, 3, true>(g, L, s);
+        }
+        break;
       case 3: if constexpr (kTma) return launch_variant<OP, T, COMP, 16, 64, 1, 2, TM, true>(g, L, s); break;
     }
   } else {  // radius 4: 10-plane queues leave no registers for pairs

@@ -45,6 +45,17 @@ static void variant_shape(int v, int r, int precision, int *ntx, int *ry, int *v
   *vx = r == 1 ? 2 : 1;
 }
 
+// Output tile width of a region ntx columns wide with halo h whose start is
+// aligned to `align` columns (the kernel's FusedShape::BX): for the
+// register/global-load variants a multiple of align when that is at least as
+// wide as the general width ntx - 2h - (align-1); the TMA variants keep the
+// general width, so that an output tile names one variant.
+int fused_tile_width(int ntx, int h, int align, bool tma) {
+  const int mis = ((-h) % align + align) % align;
+  const int aligned = (ntx - 2 * h - mis) / align * align, general = ntx - 2 * h - (align - 1);
+  return !tma && aligned >= general ? aligned : general;
+}
+
 FusedConfig make_fused_config(const Geom &g, int precision, int depth, int variant) {
   FusedConfig c{};
   if (!fused_supported(g, precision) || depth < 1 || depth > fused_max_depth(g, precision) ||
@@ -74,7 +85,7 @@ FusedConfig make_fused_config(const Geom &g, int precision, int depth, int varia
   if (smem > (size_t)227 * 1024) return FusedConfig{};
   c.depth = depth;
   c.variant = variant;
-  c.bx = ntx - 2 * depth * g.r - (align - 1);  // the region start is aligned to `align` columns
+  c.bx = fused_tile_width(ntx, depth * g.r, align, tma);
   c.by = ry - 2 * depth * g.r;
   if (c.bx <= 0 || c.by <= 0) c.depth = 0;
   return c;

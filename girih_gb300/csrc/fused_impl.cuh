@@ -179,7 +179,15 @@ struct FusedShape {
   static constexpr int H = TT * R;
   // x alignment of the region start: one x group, or 16 bytes for TMA boxes
   static constexpr int ALIGN = TMA ? (16 / (int)sizeof(ST) > VX ? 16 / (int)sizeof(ST) : VX) : VX;
-  static constexpr int BX = RW - 2 * H - (ALIGN - 1), BY = RY - 2 * H;  // output tile
+  // output tile width: without TMA a multiple of ALIGN when that loses no
+  // more columns than an arbitrary start does (every tile then starts aligned,
+  // the region start X0 - H is off by the same MIS columns in every tile, and
+  // each x group lies wholly inside or outside the output); otherwise any
+  // width with up to ALIGN-1 columns of alignment slack (fused_tile_width in
+  // fused.cu computes the same)
+  static constexpr int MIS = ((-H) % ALIGN + ALIGN) % ALIGN;
+  static constexpr int BXA = (RW - 2 * H - MIS) / ALIGN * ALIGN, BXU = RW - 2 * H - (ALIGN - 1);
+  static constexpr int BX = !TMA && BXA >= BXU ? BXA : BXU, BY = RY - 2 * H;  // output tile
   static constexpr size_t field_bytes = (size_t)2 * TT * PR * PW * sizeof(T);
   // TMA rings: NB planes of the input state (and the old state), NR planes of roc2
   static constexpr int NB = fused_tma_nb(R, TT);

@@ -44,3 +44,14 @@ def gpu_context(g, **kw):
 def max_rel(a, b, g):
     n = oracle.norms(a, b, g)
     return n[0] / n[1] if n[1] > 0 else n[0]
+
+
+def fused_block(r, w, h, depth, align):
+    """Output tile (BX, BY) of a register/global-load fused region w x h with
+    halo depth*r whose start is aligned to `align` columns (the kernel's
+    FusedShape: a multiple of align when that is at least as wide as the
+    general w - 2H - (align-1); TMA tiles always take the general width)."""
+    H = depth * r
+    mis = (-H) % align
+    bx = max((w - 2 * H - mis) // align * align, w - 2 * H - (align - 1))
+    return (bx, h - 2 * H)

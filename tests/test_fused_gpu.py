@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from girih_gb300 import gpu
-from gpu_helpers import gpu_context, max_rel, oracle_grid
+from gpu_helpers import fused_block, gpu_context, max_rel, oracle_grid
 
 pytestmark = pytest.mark.gpu
 
@@ -24,7 +24,7 @@ SMEM_MAX = 227 * 1024
 def _block(op, depth, variant):
     r = gpu.OP_INFO[op][0]
     w, h = TILE[variant]
-    return (w - 2 * depth * r - (1 if r == 1 else 0), h - 2 * depth * r)  # x pairs lose one column
+    return fused_block(r, w, h, depth, 2 if r == 1 else 1)  # radius 1: x pairs, 2-column alignment
 
 
 def _fits(variant, depth, tsz):
@@ -170,7 +170,7 @@ def test_fused_double_float_within_fp64_bound(op, variant):
         if h - 2 * depth * r <= 0:
             continue
         with gpu_context(g0.copy(), precision="fp64df", schedule="fused", fusion_depth=depth,
-                         block=(w - 2 * depth * r - pair, h - 2 * depth * r)) as ctx:
+                         block=fused_block(r, w, h, depth, 2 if pair else 1)) as ctx:
             ctx.run(nt)
             # the passes, plus the FP64 -> pair splits and the pair -> FP64 joins of the run
             split_join = (3 if gpu.OP_INFO[op][1] == 2 else 2) + 2
@@ -219,7 +219,8 @@ def test_fused_tma_variants(op, precision, variant):
         nt = 7
         ref = g0.copy().run(nt, nthreads=4)
         for depth in range(1, MAX_DEPTH[(precision, r)] + 1):
-            block = (w - 2 * depth * r - 3, h - 2 * depth * r)  # FP32 boxes start on 16 bytes: 4 columns
+            # FP32 boxes start on 16 bytes (4 columns); TMA tiles keep the general width
+            block = (w - 2 * depth * r - 3, h - 2 * depth * r)
             with gpu_context(g0.copy(), precision=precision, schedule="fused", fusion_depth=depth,
                              block=block) as ctx:
                 with gpu_context(g0.copy(), precision=precision, schedule="fused", fusion_depth=depth,

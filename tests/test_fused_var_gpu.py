@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from girih_gb300 import gpu
-from gpu_helpers import gpu_context, max_rel, oracle_grid
+from gpu_helpers import fused_block, gpu_context, max_rel, oracle_grid
 
 pytestmark = pytest.mark.gpu
 
@@ -45,7 +45,7 @@ def test_fused_var_fp32_all_depths(op, variant):
     r = gpu.OP_INFO[op][0]
     w, h = (64, 32) if variant == 0 else (32, 64)
     for depth in range(1, _max_depth(op) + 1):
-        block = (w - 2 * depth * r - (1 if r == 1 else 0), h - 2 * depth * r)
+        block = fused_block(r, w, h, depth, 2 if r == 1 else 1)
         g = g0.copy()
         with gpu_context(g, precision="fp32", schedule="fused", fusion_depth=depth, block=block) as ctx:
             info = ctx.info()

@@ -276,18 +276,29 @@ def run_ours(args, wl, rank, world, local):
             ectx.run(nt)
             ectx.download(host[0].data_ptr(), None)
         barrier_sync()
+        # each call returns after its stream work completed, so host clocks
+        # between the calls split the step into its phases
+        ph = {"upload": 0.0, "run": 0.0, "download": 0.0}
         t0 = time.perf_counter()
         for _ in range(args.steps):
+            a = time.perf_counter()
             ectx.upload(host[0].data_ptr(), host[1].data_ptr(), u3, coefs if not op_info[3] else coefs.data_ptr())
+            b = time.perf_counter()
             ectx.run(nt)
+            c = time.perf_counter()
             ectx.download(host[0].data_ptr(), None)
+            d = time.perf_counter()
+            ph["upload"] += b - a
+            ph["run"] += c - b
+            ph["download"] += d - c
         barrier_sync()
         wall = max_over_ranks(time.perf_counter() - t0, "cuda")
         nbytes = host[0].numel() * 8
         e2e = {"value": world * args.steps * lups / wall / 1e9, "unit": "GLUP/s",
                "h2d_bytes_per_step": nbytes * (3 if u3 else 2) + (nbytes * op_info[2] if op_info[3] else 0),
                "d2h_bytes_per_step": nbytes,
-               "host_arrays": "pinned FP64 (reference real_t=double layout)"}
+               "host_arrays": "pinned FP64 (reference real_t=double layout)",
+               "phases_ms_per_step": {k: 1e3 * v / args.steps for k, v in ph.items()}}
         ectx.close()
     for c in ctxs.values():
         c.close()

@@ -1,13 +1,14 @@
-"""BASELINE configurations as parity cases (reduced sizes where the CPU oracle
+"""The benchmark workloads as parity cases (reduced sizes where the CPU oracle
 must follow), plus size-independent properties at the full 512^3 size.
 
-config 1: operator 1, 128^3, nt=50, seed 0, U(0,1), default coefficients.
-config 2: operator 8 (7-point leapfrog), seed 1, U(0,1) -- full size in the bench;
+star7 Jacobi 128^3: operator 1, nt=50, seed 0, U(0,1), default coefficients.
+star7 leapfrog: operator 8, seed 1, U(0,1) -- 512^3 / nt=500 in the bench;
           96^3 / nt=100 here against the oracle, and exact power-of-two
           linearity at 512^3.
-config 3: operator 0, seed 2, U(-1,1), stable 8th-order weights, roc2 U(0.05,0.15);
-          72^3 here, errors reported at nt = 50 (and 100 for FP32).
-config 4: operators 5 and 4, seed 3, coefficients U(0.01, 0.1/r); 48^3 here.
+star25 leapfrog: operator 0, seed 2, U(-1,1), stable 8th-order weights, roc2
+          U(0.05,0.15); 72^3 here, errors reported at nt = 50 (and 100 for FP32).
+variable coefficients: operators 5 and 4, seed 3, coefficients U(0.01, 0.1/r);
+          48^3 here.
 """
 import numpy as np
 import pytest
@@ -28,7 +29,7 @@ def _seeded(op, n, seed, f, roc2=(0.0, 0.0), c=(0.0, 0.0), coefs=None):
     return g
 
 
-def test_config1_exact_fp64_bit_identical():
+def test_star7_jacobi_128_exact_fp64_bit_identical():
     g = _seeded(1, 128, 0, (0.0, 1.0))
     with gpu_context(g.copy(), precision="fp64", exact=True) as ctx:
         ctx.run(50)
@@ -38,7 +39,7 @@ def test_config1_exact_fp64_bit_identical():
     np.testing.assert_array_equal(u2, g.U2)
 
 
-def test_config2_reduced_all_forms():
+def test_star7_leapfrog_reduced_all_forms():
     g0 = _seeded(8, 96, 1, (0.0, 1.0), roc2=(0.5, 1.5), coefs=LAP2)
     ref = g0.copy().run(100, nthreads=8)
     for prec, sched, tol in (("fp64", "plain", 1e-12), ("fp64", "fused", 1e-12), ("fp64df", "fused", 1e-12),
@@ -52,7 +53,7 @@ def test_config2_reduced_all_forms():
 
 @pytest.mark.parametrize("prec,sched,tol", [("fp64", "plain", 1e-12), ("fp64", "fused", 1e-12),
                                             ("fp32", "fused", 1e-5), ("mixed", "fused", 1e-5)])
-def test_config3_reduced(prec, sched, tol):
+def test_star25_leapfrog_reduced(prec, sched, tol):
     g0 = _seeded(0, 72, 2, (-1.0, 1.0), roc2=(0.05, 0.15), coefs=LAP8)
     ref = g0.copy()
     with gpu_context(g0.copy(), precision=prec, schedule=sched) as ctx:
@@ -65,7 +66,7 @@ def test_config3_reduced(prec, sched, tol):
 
 
 @pytest.mark.parametrize("op", [5, 4])
-def test_config4_reduced(op):
+def test_var_coef_reduced(op):
     r = gpu.OP_INFO[op][0]
     g0 = _seeded(op, 48, 3, (0.0, 1.0), c=(0.01, 0.1 / r))
     ref = g0.copy().run(20, nthreads=8)

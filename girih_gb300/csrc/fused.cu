@@ -63,7 +63,8 @@ FusedConfig make_fused_config(const Geom &g, int precision, int depth, int varia
     return c;
   int ntx, ry, vx;
   variant_shape(variant, g.r, precision, &ntx, &ry, &vx);
-  if (variant == 2 && g.r == 1 && depth == 4 && precision != GIRIH_FP64_DF) vx = 4;  // x quads at depth 4
+  if (variant == 2 && precision != GIRIH_FP64_DF && ((g.r == 1 && depth == 4) || (g.r == 4 && depth == 1)))
+    vx = 4;  // x quads: radius 1 at depth 4, radius 4 at depth 1
   // double-buffered shared memory of all levels (rows padded by r), plus the TMA
   // rings of the TMA variants, must fit one CTA (227 KiB)
   const size_t tsz = (precision == GIRIH_FP64 || precision == GIRIH_FP64_DF) ? 8 : 4;

@@ -45,7 +45,13 @@ template <class T> constexpr int batch_tmax(int r) { return r == 4 ? 2 : (sizeof
 template <int OP, class T, bool COMP, int TT>
 __device__ __forceinline__ void run_tile(const FusedArgs<T> &a, int4 w, int tid, unsigned char *sm) {
   using M = BatchMap<OP>;
-  fused_tile<OP, T, COMP, TT, M::NTX, M::NTY, M::CY, M::VX>(a, w.y, w.z, w.w, tid % M::NTX, tid / M::NTX, sm);
+  if constexpr (OpTraits<OP>::R == 4 && TT == 1 && sizeof(T) == 4) {
+    // radius 4, depth 1: x quads, 16x32 threads, one row each -- the same 64 x 32
+    // region and output tile (the quads' 4-column alignment costs no column)
+    fused_tile<OP, T, COMP, TT, 16, 32, 1, 4>(a, w.y, w.z, w.w, tid % 16, tid / 16, sm);
+  } else {
+    fused_tile<OP, T, COMP, TT, M::NTX, M::NTY, M::CY, M::VX>(a, w.y, w.z, w.w, tid % M::NTX, tid / M::NTX, sm);
+  }
 }
 
 template <class T, bool COMP>
@@ -107,6 +113,7 @@ template <class T, bool COMP> size_t batched_smem() {
     upd(FusedShape<1, T, COMP, 2, 32, 16, 2, 2>::smem_bytes);
   }
   upd(FusedShape<0, T, COMP, 2, 64, 8, 4, 1>::smem_bytes);
+  upd(FusedShape<0, T, COMP, 1, 16, 32, 1, 4>::smem_bytes);
   return m;
 }
 

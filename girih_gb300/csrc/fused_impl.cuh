@@ -152,6 +152,43 @@ template <int R, class T, int QL, int BASE, int VX, int V> struct FusedAcc {
   __device__ __forceinline__ T z(int d) const { return q[V][qslot<QL>(BASE + d)]; }
 };
 
+// Variable coefficients of one column of a thread's x group, preloaded for the
+// whole group (the accessor of apply_op; the element index is not needed).
+template <class T, int NC, int VX, int V> struct CoefGroup {
+  const T (&cf)[NC][VX];
+  __device__ __forceinline__ T operator()(int m, int64_t) const { return cf[m][V]; }
+};
+
+// Load the nc coefficients of VX consecutive columns starting at element e:
+// one vector load per array (FP32: 4*VX bytes; BF16: 2*VX bytes, scaled).
+template <class T, bool BF16, int NC, int VX>
+__device__ __forceinline__ void load_coef_group(const void *coef, int64_t stride, const float *scale, int e,
+                                                T (&cf)[NC][VX]) {
+#pragma unroll
+  for (int m = 0; m < NC; m++) {
+    if constexpr (BF16) {
+      const __nv_bfloat16 *p = static_cast<const __nv_bfloat16 *>(coef) + m * stride + e;
+      const float sc = __ldg(scale + m);
+      if constexpr (VX == 1) {
+        cf[m][0] = __bfloat162float(p[0]) * sc;
+      } else {
+        union {
+          typename VecBits<2 * VX>::type v;
+          __nv_bfloat16 h[VX];
+        } u;
+        u.v = __ldg(reinterpret_cast<const decltype(u.v) *>(p));
+#pragma unroll
+        for (int k = 0; k < VX; k++) cf[m][k] = __bfloat162float(u.h[k]) * sc;
+      }
+    } else {
+      VecU<T, VX> u;
+      u.v = __ldg(reinterpret_cast<const decltype(u.v) *>(static_cast<const T *>(coef) + m * stride + e));
+#pragma unroll
+      for (int k = 0; k < VX; k++) cf[m][k] = u.e[k];
+    }
+  }
+}
+
 template <class F, int... I>
 __device__ __forceinline__ void static_for_impl(F &f, std::integer_sequence<int, I...>) {
   (f(std::integral_constant<int, I>{}), ...);
@@ -284,12 +321,6 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
   // variable coefficients (operators 2-5): full precision, or BF16 with a
   // per-array scale in the mixed form (COMP selects BF16 for these operators)
   constexpr bool VAR = OpTraits<OP>::VAR;
-  using CoefF = typename std::conditional<VAR && COMP, CoefBF16, CoefFull<T>>::type;
-  CoefF coeff{};
-  if constexpr (VAR) {
-    if constexpr (COMP) coeff = CoefBF16{static_cast<const __nv_bfloat16 *>(a.coef), g.elems, a.cscale};
-    else coeff = CoefFull<T>{static_cast<const T *>(a.coef), g.elems};
-  }
 
   // source point: its plane, and per row the position inside this thread's
   // x group (-1: not this thread's)
@@ -439,6 +470,11 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
               yv[R + d - 1][v] = dn.e[v];
             }
           }
+          // variable coefficients of the group at this plane: one vector load per
+          // array (the row is interior, so the whole group lies inside the array)
+          constexpr int NCF = VAR ? OpTraits<OP>::NC : 1;
+          T cf[NCF][VX];
+          if constexpr (VAR) load_coef_group<T, COMP, NCF, VX>(a.coef, g.elems, a.cscale, poff + col[c], cf);
           // x neighbours outside the group: the neighbouring groups as two vector loads
           Pack<T, VX> xlp, xrp;
           if constexpr (fused_x_groups(R, VX)) {
@@ -481,10 +517,8 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
                 cand = apply_op<OP, FastArith>(cc, none, 0, acc, uold, r2);
               }
             } else if constexpr (VAR) {
-              // coefficients exist at interior points only: inactive points
-              // (halo, outside the level's band or plane range) read element 0
-              const int ci = on ? poff + col[c] + V : 0;
-              cand = apply_op<OP, FastArith>(cc, coeff, (int64_t)ci, acc, T(0), T(0));
+              CoefGroup<T, NCF, VX, V> cg{cf};
+              cand = apply_op<OP, FastArith>(cc, cg, 0, acc, T(0), T(0));
             } else {
               CoefFull<T> none{nullptr, 0};
               cand = apply_op<OP, FastArith>(cc, none, 0, acc, T(0), T(0));

@@ -31,7 +31,8 @@ int fused_max_depth(const Geom &g, int precision) {
 //   double-float: one column per thread in variants 0 = 64 x 32 (64x16 threads,
 //   2 rows), 1 = 32 x 32 (32x16 threads, 2 rows), 2 = 64 x 16 (64x16 threads,
 //   1 row); x pairs (radius 1) in variants 3 = 64 x 32 (32x16 threads, 2 rows)
-//   and 4 = 32 x 64 (16x64 threads, 1 row).
+//   and 4 = 32 x 64 (16x64 threads, 1 row).  (Double-float x quads, 16x32
+//   threads, measured 143 vs 163 GLUP/s for x pairs at depth 2.)
 static void variant_shape(int v, int r, int precision, int *ntx, int *ry, int *vx) {
   if (precision == GIRIH_FP64_DF) {
     static const int shape[5][3] = {{64, 32, 1}, {32, 32, 1}, {64, 16, 1}, {64, 32, 2}, {32, 64, 2}};
@@ -48,12 +49,12 @@ static void variant_shape(int v, int r, int precision, int *ntx, int *ry, int *v
 // Output tile width of a region ntx columns wide with halo h whose start is
 // aligned to `align` columns (the kernel's FusedShape::BX): for the
 // register/global-load variants a multiple of align when that is at least as
-// wide as the general width ntx - 2h - (align-1); the TMA variants keep the
-// general width, so that an output tile names one variant.
-int fused_tile_width(int ntx, int h, int align, bool tma) {
+// wide as the general width ntx - 2h - (align-1); the TMA and double-float
+// variants keep the general width, so that an output tile names one variant.
+int fused_tile_width(int ntx, int h, int align, bool general_only) {
   const int mis = ((-h) % align + align) % align;
   const int aligned = (ntx - 2 * h - mis) / align * align, general = ntx - 2 * h - (align - 1);
-  return !tma && aligned >= general ? aligned : general;
+  return !general_only && aligned >= general ? aligned : general;
 }
 
 FusedConfig make_fused_config(const Geom &g, int precision, int depth, int variant) {
@@ -86,7 +87,7 @@ FusedConfig make_fused_config(const Geom &g, int precision, int depth, int varia
   if (smem > (size_t)227 * 1024) return FusedConfig{};
   c.depth = depth;
   c.variant = variant;
-  c.bx = fused_tile_width(ntx, depth * g.r, align, tma);
+  c.bx = fused_tile_width(ntx, depth * g.r, align, tma || precision == GIRIH_FP64_DF);
   c.by = ry - 2 * depth * g.r;
   if (c.bx <= 0 || c.by <= 0) c.depth = 0;
   return c;

@@ -233,7 +233,10 @@ struct FusedShape {
   // fused.cu computes the same)
   static constexpr int MIS = ((-H) % ALIGN + ALIGN) % ALIGN;
   static constexpr int BXA = (RW - 2 * H - MIS) / ALIGN * ALIGN, BXU = RW - 2 * H - (ALIGN - 1);
-  static constexpr int BX = !TMA && BXA >= BXU ? BXA : BXU, BY = RY - 2 * H;  // output tile
+  // (double-float tiles keep the general width too: their one-column and x-group
+  // variants share regions, and an output tile names one variant)
+  static constexpr bool ALIGNED_W = !TMA && !std::is_same<T, Df64>::value;
+  static constexpr int BX = ALIGNED_W && BXA >= BXU ? BXA : BXU, BY = RY - 2 * H;  // output tile
   static constexpr size_t field_bytes = (size_t)2 * TT * PR * PW * sizeof(T);
   // TMA rings: NB planes of the input state (and the old state), NR planes of roc2
   static constexpr int NB = fused_tma_nb(R, TT);

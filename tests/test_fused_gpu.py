@@ -162,15 +162,16 @@ def test_fused_double_float_within_fp64_bound(op, variant):
     g0 = oracle_grid(op, *_shape(op), seed=17)
     nt = 9
     ref = g0.copy().run(nt, nthreads=4)
-    # double-float regions: one column per thread (0-2), x pairs (3, 4; one column lost to alignment)
-    w, h, pair = {0: (64, 32, 0), 1: (32, 32, 0), 2: (64, 16, 0), 3: (64, 32, 1), 4: (32, 64, 1)}[variant]
+    # double-float regions: one column per thread (0-2), x pairs (3, 4); the output tile
+    # keeps the general width w - 2H - (group - 1)
+    w, h, grp = {0: (64, 32, 1), 1: (32, 32, 1), 2: (64, 16, 1), 3: (64, 32, 2), 4: (32, 64, 2)}[variant]
     if variant >= 2 and r != 1:
         return  # radius 1 only
     for depth in range(1, (3 if r == 1 else 2) + 1):
         if h - 2 * depth * r <= 0:
             continue
         with gpu_context(g0.copy(), precision="fp64df", schedule="fused", fusion_depth=depth,
-                         block=fused_block(r, w, h, depth, 2 if pair else 1)) as ctx:
+                         block=(w - 2 * depth * r - (grp - 1), h - 2 * depth * r)) as ctx:
             ctx.run(nt)
             # the passes, plus the FP64 -> pair splits and the pair -> FP64 joins of the run
             split_join = (3 if gpu.OP_INFO[op][1] == 2 else 2) + 2

@@ -152,12 +152,12 @@ def run_ours(args, wl, rank, world, local):
     torch.cuda.set_device(local)
     n, nt, op = wl["n"], wl["nt"], wl["op"]
     lups = float(n) ** 3 * (2 * ((nt + 1) // 2))
-    if gpu.OP_INFO[op][3]:  # variable coefficients: FP32-field forms are fused
+    if gpu.OP_INFO[op][3]:  # variable coefficients: the mixed form streams them in the x-quad plain sweep
         forms = {
             "plain64": dict(precision="fp64", schedule="plain"),
-            "mixedplain": dict(precision="mixed", schedule="plain"),
+            "mixed": dict(precision="mixed", schedule="plain"),
             "fused32": dict(precision="fp32", schedule="fused"),
-            "mixed": dict(precision="mixed", schedule="fused"),
+            "mixedfused": dict(precision="mixed", schedule="fused"),
         }
     else:
         forms = {

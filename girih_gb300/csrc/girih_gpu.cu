@@ -483,10 +483,11 @@ int girih_gpu_create(girih_gpu_ctx **out, const girih_gpu_desc *d) {
   if (sched != GIRIH_SCHED_PLAIN && untuned && cached_choice(c->g, d->precision, &tc)) {
     if (d->schedule == GIRIH_SCHED_AUTO) c->sched = sched = tc.sched;
     if (tc.sched == GIRIH_SCHED_FUSED) c->fcfg = make_fused_config(c->g, d->precision, tc.depth, tc.variant);
-  } else if (d->schedule == GIRIH_SCHED_AUTO && c->g.var && c->g.r == 4) {
-    // untuned default: at radius 4 the overlapped tiles recompute ~2x the points,
-    // which costs the variable-coefficient operator more than the coefficient
-    // bytes it saves; only a tuning run that measured otherwise selects fusion
+  } else if (d->schedule == GIRIH_SCHED_AUTO && c->g.var) {
+    // untuned default for variable coefficients: the x-quad plain sweep streams
+    // them near the HBM roof, while the overlapped fused tiles recompute 1.2x
+    // (radius 1) to 2x (radius 4) the points; only a tuning run that measured
+    // otherwise selects fusion
     c->sched = sched = GIRIH_SCHED_PLAIN;
   }
   if (sched == GIRIH_SCHED_FUSED && !c->fcfg.depth) {

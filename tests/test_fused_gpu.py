@@ -129,7 +129,7 @@ def test_fused_requires_equal_halos():
 
 def test_auto_schedule_picks_fused_where_provided():
     for op, prec, want in ((1, "fp64", gpu.FUSED), (8, "fp64", gpu.FUSED), (0, "fp64", gpu.FUSED),
-                           (5, "fp64", gpu.PLAIN), (5, "mixed", gpu.FUSED), (4, "mixed", gpu.PLAIN)):
+                           (5, "fp64", gpu.PLAIN), (5, "mixed", gpu.PLAIN), (4, "mixed", gpu.PLAIN)):
         with gpu.Context(op, 32, 32, 32, precision=prec, schedule="auto") as ctx:
             assert ctx.info()["schedule"] == want, (op, prec)
 

@@ -78,6 +78,19 @@ int size_class(const Geom &g) {
   return (int)std::floor(std::log2(pts > 1 ? pts : 1));
 }
 
+// Untuned default of the auto schedule, from measurements at 384^3-512^3:
+// FP64 arithmetic is bound by the FP64 pipe, where fusion only adds the halo
+// recomputation (operator 8: 51 plain vs 36 fused GLUP/s); double-float
+// arithmetic exists in the fused passes only; in FP32 fields fusion wins for
+// the radius-1 constant operators (operator 8: 512 vs 356, operator 1: 722 vs
+// 609) and loses where the overlapped tiles recompute many points or stream
+// coefficient arrays (radius 4: 176 vs 237; variable coefficients: 200 vs 268).
+bool auto_prefers_fused(const Geom &g, int precision) {
+  if (precision == GIRIH_FP64_DF) return true;
+  if (precision == GIRIH_FP64) return false;
+  return !g.var && g.r == 1;
+}
+
 bool cached_choice(const Geom &g, int precision, TuneChoice *out) {
   std::lock_guard<std::mutex> lock(g_tune_mutex);
   auto it = g_tune_cache.find(std::make_tuple(g.op, precision, size_class(g)));
@@ -483,12 +496,8 @@ int girih_gpu_create(girih_gpu_ctx **out, const girih_gpu_desc *d) {
   if (sched != GIRIH_SCHED_PLAIN && untuned && cached_choice(c->g, d->precision, &tc)) {
     if (d->schedule == GIRIH_SCHED_AUTO) c->sched = sched = tc.sched;
     if (tc.sched == GIRIH_SCHED_FUSED) c->fcfg = make_fused_config(c->g, d->precision, tc.depth, tc.variant);
-  } else if (d->schedule == GIRIH_SCHED_AUTO && c->g.var) {
-    // untuned default for variable coefficients: the x-quad plain sweep streams
-    // them near the HBM roof, while the overlapped fused tiles recompute 1.2x
-    // (radius 1) to 2x (radius 4) the points; only a tuning run that measured
-    // otherwise selects fusion
-    c->sched = sched = GIRIH_SCHED_PLAIN;
+  } else if (d->schedule == GIRIH_SCHED_AUTO && !auto_prefers_fused(c->g, d->precision)) {
+    c->sched = sched = GIRIH_SCHED_PLAIN;  // only a tuning run that measured otherwise selects fusion
   }
   if (sched == GIRIH_SCHED_FUSED && !c->fcfg.depth) {
     c->fcfg = choose_fused_config(c->g, d->precision, d->fusion_depth, d->block_x, d->block_y);

@@ -127,8 +127,13 @@ def test_fused_requires_equal_halos():
     np.testing.assert_array_equal(u1, g.copy().run(4).U1)
 
 
-def test_auto_schedule_picks_fused_where_provided():
-    for op, prec, want in ((1, "fp64", gpu.FUSED), (8, "fp64", gpu.FUSED), (0, "fp64", gpu.FUSED),
+def test_auto_schedule_untuned_defaults():
+    """Untuned auto: fused where it measured faster (FP32 fields, radius-1 constant
+    operators; double-float), plain elsewhere (FP64 arithmetic, radius 4,
+    variable coefficients)."""
+    for op, prec, want in ((1, "fp64", gpu.PLAIN), (8, "fp64", gpu.PLAIN), (0, "fp64", gpu.PLAIN),
+                           (8, "fp64df", gpu.FUSED), (1, "mixed", gpu.FUSED), (8, "mixed", gpu.FUSED),
+                           (8, "fp32", gpu.FUSED), (0, "mixed", gpu.PLAIN),
                            (5, "fp64", gpu.PLAIN), (5, "mixed", gpu.PLAIN), (4, "mixed", gpu.PLAIN)):
         with gpu.Context(op, 32, 32, 32, precision=prec, schedule="auto") as ctx:
             assert ctx.info()["schedule"] == want, (op, prec)

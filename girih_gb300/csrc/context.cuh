@@ -44,6 +44,7 @@ struct girih_gpu_ctx {
   // TMA tensor maps of the four field buffers and roc2 (index 4), per TMA variant (2, 3)
   CUtensorMap tmaps[5][2];
   bool tmap_ok[5][2] = {{false, false}, {false, false}, {false, false}, {false, false}, {false, false}};
+  int tmap_box[5][2][2] = {};  // box (x, y) each cached map was encoded with: a variant's box can change with depth
 };
 
 namespace girih {

@@ -66,6 +66,10 @@ FusedConfig make_fused_config(const Geom &g, int precision, int depth, int varia
   variant_shape(variant, g.r, precision, &ntx, &ry, &vx);
   if (variant == 2 && precision != GIRIH_FP64_DF && ((g.r == 1 && depth == 4) || (g.r == 4 && depth == 1)))
     vx = 4;  // x quads: radius 1 at depth 4, radius 4 at depth 1
+  if (variant == 3 && precision != GIRIH_FP64_DF && g.r == 1 && depth <= 2) {
+    ntx = 64;  // 64 x 64 region with x quads
+    vx = 4;
+  }
   // double-buffered shared memory of all levels (rows padded by r), plus the TMA
   // rings of the TMA variants, must fit one CTA (227 KiB)
   const size_t tsz = (precision == GIRIH_FP64 || precision == GIRIH_FP64_DF) ? 8 : 4;
@@ -77,7 +81,7 @@ FusedConfig make_fused_config(const Geom &g, int precision, int depth, int varia
   size_t smem = (size_t)2 * depth * (ntx + 2 * rp) * (ry + 2 * g.r) * tsz;
   int align = vx;
   if (tma) {
-    const int nb = fused_tma_nb(g.r, depth), nr = fused_tma_nr(g.r, depth, nb);
+    const int nb = fused_tma_nb(g.r, depth, ntx * ry), nr = fused_tma_nr(g.r, depth, nb);
     const size_t plane = (size_t)ntx * ry * tsz;
     smem = (smem + 127) / 128 * 128 + nb * plane + (g.to == 2 ? (nb + nr) * plane : 0) + nb * 8;
     align = 16 / (int)tsz > vx ? 16 / (int)tsz : vx;

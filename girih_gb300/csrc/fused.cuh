@@ -14,7 +14,9 @@ enum FusedVariant { FV_64x32_512 = 0, FV_32x64_1024 = 1, FV_64x32_512_TMA = 2, F
 
 // TMA ring depths: NB planes of the input (and old) state in flight, NR planes
 // of roc2 (level l reads roc2 (l-1)*(R+1) planes after level 1 did).
-__host__ __device__ constexpr int fused_tma_nb(int r, int tt) { return (r == 4 || tt >= 4) ? 2 : 4; }
+__host__ __device__ constexpr int fused_tma_nb(int r, int tt, int area) {
+  return (r == 4 || tt >= 4 || area > 2048) ? 2 : 4;
+}
 __host__ __device__ constexpr int fused_tma_nr(int r, int tt, int nb) {
   int need = (tt - 1) * (r + 1) + nb, p = 1;
   while (p < need) p *= 2;
@@ -38,6 +40,7 @@ struct FusedLaunch {
   unsigned *range_flag;    // bit 0: a value left the FP32 exponent range (double-float);
                            // bit 1: a TMA copy did not complete within the wait bound
   const void *tma_cur, *tma_prev, *tma_roc2;  // host CUtensorMap objects (TMA variants)
+  int tma_box_w, tma_box_h;                   // the box the maps were encoded with
   const void *coef;        // variable coefficients (device layout arrays)
   const float *cscale;     // per-array scales of BF16 coefficients (mixed form)
   const double *src;       // source values per step (null: no source point)

@@ -191,7 +191,7 @@ struct FusedShape {
   static constexpr int BX = ALIGNED_W && BXA >= BXU ? BXA : BXU, BY = RY - 2 * H;  // output tile
   static constexpr size_t field_bytes = (size_t)2 * TT * PR * PW * sizeof(T);
   // TMA rings: NB planes of the input state (and the old state), NR planes of roc2
-  static constexpr int NB = fused_tma_nb(R, TT);
+  static constexpr int NB = fused_tma_nb(R, TT, RW * RY);
   static constexpr int NR = fused_tma_nr(R, TT, NB);
   static constexpr size_t plane_bytes = (size_t)RW * RY * sizeof(ST);
   static constexpr size_t off_cur = (field_bytes + 127) / 128 * 128;
@@ -645,6 +645,8 @@ cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
   a.write_prev = L.write_prev;
   if constexpr (TMA) {
     if (!L.tma_cur || !L.tma_roc2 || !L.tma_prev) return cudaErrorInvalidValue;
+    // the copies must fill exactly the ring slots this shape sizes
+    if (L.tma_box_w != S::RW || L.tma_box_h != S::RY) return cudaErrorInvalidValue;
     TmaMaps maps;
     maps.cur = *static_cast<const CUtensorMap *>(L.tma_cur);
     maps.prev = *static_cast<const CUtensorMap *>(L.tma_prev);
@@ -714,7 +716,12 @@ cudaError_t launch_fused_op_impl(const Geom &g, const FusedConfig &cfg, const Fu
           return launch_variant<OP, T, COMP, 32, 16, 2, 2, 3, true>(g, L, s);
         }
         break;
-      case 3: if constexpr (kTma) return launch_variant<OP, T, COMP, 16, 64, 1, 2, TM, true>(g, L, s); break;
+      case 3:  // depth <= 2: 64 x 64 region with x quads, 1024 threads; deeper: 32 x 64 with x pairs
+        if constexpr (kTma) {
+          if (cfg.depth <= 2) return launch_variant<OP, T, COMP, 16, 64, 1, 4, 2, true>(g, L, s);
+          return launch_variant<OP, T, COMP, 16, 64, 1, 2, TM, true>(g, L, s);
+        }
+        break;
     }
   } else {  // radius 4: 10-plane queues leave no registers for wider groups beyond depth 1
     switch (cfg.variant) {

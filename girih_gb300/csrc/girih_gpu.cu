@@ -257,7 +257,10 @@ EncodeTiledFn encode_tiled() {
 const CUtensorMap *tensor_map(girih_gpu_ctx *c, int arr, const void *base) {
   const int v = c->fcfg.variant - 2;
   if (v < 0 || v > 1) return nullptr;
-  if (!c->tmap_ok[arr][v]) {
+  // re-encode when the box changed: a TMA copy of another width would overrun
+  // (or under-fill) the ring slots the kernel sized for its own region
+  if (!c->tmap_ok[arr][v] || c->tmap_box[arr][v][0] != c->fcfg.box_w || c->tmap_box[arr][v][1] != c->fcfg.box_h) {
+    c->tmap_ok[arr][v] = false;
     EncodeTiledFn fn = encode_tiled();
     if (!fn) return nullptr;
     const Geom &g = c->g;
@@ -270,6 +273,8 @@ const CUtensorMap *tensor_map(girih_gpu_ctx *c, int arr, const void *base) {
                     CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return nullptr;
     c->tmap_ok[arr][v] = true;
+    c->tmap_box[arr][v][0] = c->fcfg.box_w;
+    c->tmap_box[arr][v][1] = c->fcfg.box_h;
   }
   return &c->tmaps[arr][v];
 }
@@ -390,6 +395,8 @@ int issue_steps_impl(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *
       L.tma_prev = tensor_map(c, *iu1, c->f[*iu1]);
       L.tma_cur = tensor_map(c, *iu2, c->f[*iu2]);
       L.tma_roc2 = c->g.to == 2 ? tensor_map(c, 4, c->roc2) : L.tma_cur;
+      L.tma_box_w = c->fcfg.box_w;
+      L.tma_box_h = c->fcfg.box_h;
       if (!L.tma_prev || !L.tma_cur || !L.tma_roc2)
         return fail(GIRIH_GPU_ECUDA, "TMA tensor map encoding failed");
     }

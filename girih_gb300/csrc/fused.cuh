@@ -7,13 +7,17 @@ namespace girih {
 // Thread-block shapes of the fused kernel.  A CTA covers an input region of
 // columns (tile + halo of depth*R on every side); each thread owns VX x columns
 // and CY rows of it and streams the whole z range.  Variants 2 and 3 are
-// variants 0 and 1 with the input planes staged into shared memory by TMA.
-// Tile variants of the FP32/FP64 forms (the double-float form numbers its own
-// five shapes 0-4, see variant_shape in fused.cu).
+// variants 0 and 1 with the input planes staged into shared memory by TMA
+// (FP32 storage; variant 2 switches to x quads at radius-1 depth 4 and
+// radius-4 depth 1, variant 3 to a 64 x 64 region with x quads at radius-1
+// depth <= 2).  The double-float form numbers its own five shapes 0-4, see
+// variant_shape in fused.cu.
 enum FusedVariant { FV_64x32_512 = 0, FV_32x64_1024 = 1, FV_64x32_512_TMA = 2, FV_32x64_1024_TMA = 3, FV_COUNT = 5 };
 
-// TMA ring depths: NB planes of the input (and old) state in flight, NR planes
-// of roc2 (level l reads roc2 (l-1)*(R+1) planes after level 1 did).
+// TMA ring depths: NB planes of the input (and old) state in flight (two for
+// deep passes and large regions, whose rings would not fit shared memory
+// otherwise), NR planes of roc2 (level l reads roc2 (l-1)*(R+1) planes after
+// level 1 did).
 __host__ __device__ constexpr int fused_tma_nb(int r, int tt, int area) {
   return (r == 4 || tt >= 4 || area > 2048) ? 2 : 4;
 }
@@ -37,8 +41,8 @@ struct FusedLaunch {
   int steps;               // <= config depth
   int write_prev;          // time order 1: write state t+steps-1 (last pass only)
   double cc[5];
-  unsigned *range_flag;    // bit 0: a value left the FP32 exponent range (double-float);
-                           // bit 1: a TMA copy did not complete within the wait bound
+  unsigned *range_flag;    // bit 1: a TMA copy did not complete within the wait bound
+                           // (bit 0, a value outside the FP32 range, is set by the double-float split)
   const void *tma_cur, *tma_prev, *tma_roc2;  // host CUtensorMap objects (TMA variants)
   int tma_box_w, tma_box_h;                   // the box the maps were encoded with
   const void *coef;        // variable coefficients (device layout arrays)

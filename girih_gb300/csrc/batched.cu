@@ -225,6 +225,7 @@ void fill_args(BatchGridArgs<T> &ga, const girih_gpu_ctx *c, int prev, int cur, 
   ga.a.out_prev = static_cast<T *>(c->f[oprev]);
   ga.a.out_cur = static_cast<T *>(c->f[ocur]);
   for (int m = 0; m < 5; m++) ga.a.cc[m] = c->cc[m];
+  split_coefs(ga.a.cc, ga.a.cch, ga.a.ccl);
   ga.a.zchunk = zchunk;
   ga.a.write_prev = write_prev;
   ga.op = c->g.op;

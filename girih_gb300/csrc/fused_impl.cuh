@@ -38,6 +38,7 @@ template <class S> struct FusedArgs {
   const S *prev, *cur, *roc2;
   S *out_prev, *out_cur;
   double cc[5];
+  float cch[5], ccl[5];  // cc split on the host: hi = nearest FP32, lo = nearest FP32 of the rest
   int zchunk;
   int write_prev;
   unsigned *range_flag;  // error flags (bit 1: a TMA copy timed out)
@@ -60,6 +61,22 @@ template <class S, class T> __device__ __forceinline__ S to_storage(T v) {
   if constexpr (std::is_same<T, S>::value) return v;
   else return (S)v;
 }
+// Constant coefficient m in the compute type, from the host-split copies (no
+// FP64 conversion in the kernel, which the compiler may otherwise repeat inside
+// the z loop on the scarce FP64 pipe instead of holding the value).
+template <class T, class S> __device__ __forceinline__ T coef_arg(const FusedArgs<S> &a, int m) {
+  if constexpr (std::is_same<T, Df64>::value) return Df64(a.cch[m], a.ccl[m]);
+  else if constexpr (std::is_same<T, float>::value) return a.cch[m];
+  else return (T)a.cc[m];
+}
+
+inline void split_coefs(const double *cc, float *hi, float *lo) {
+  for (int m = 0; m < 5; m++) {
+    hi[m] = (float)cc[m];
+    lo[m] = (float)(cc[m] - (double)hi[m]);
+  }
+}
+
 template <class T> __device__ __forceinline__ T coef_to_compute(double c) {
   if constexpr (std::is_same<T, Df64>::value) {
     const float h = __double2float_rn(c);
@@ -272,7 +289,7 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
 
   T cc[5];
 #pragma unroll
-  for (int m = 0; m < 5; m++) cc[m] = coef_to_compute<T>(a.cc[m]);
+  for (int m = 0; m < 5; m++) cc[m] = coef_arg<T>(a, m);
   // variable coefficients (operators 2-5): full precision, or BF16 with a
   // per-array scale in the mixed form (COMP selects BF16 for these operators)
   constexpr bool VAR = OpTraits<OP>::VAR;
@@ -634,6 +651,7 @@ cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
   a.out_prev = static_cast<ST *>(L.out_prev);
   a.out_cur = static_cast<ST *>(L.out_cur);
   for (int m = 0; m < 5; m++) a.cc[m] = L.cc[m];
+  split_coefs(a.cc, a.cch, a.ccl);
   a.range_flag = L.range_flag;
   a.coef = L.coef;
   a.cscale = L.cscale;

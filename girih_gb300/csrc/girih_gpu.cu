@@ -816,25 +816,26 @@ int girih_gpu_autotune(girih_gpu_ctx *c, int trial_steps, girih_gpu_info_t *chos
     for (int b = 2; b < 4; b++)  // spare buffers carry the fixed halo
       CK(cudaMemcpyAsync(c->f[b], c->f[c->iu2], (size_t)g.elems * c->tsz, cudaMemcpyDeviceToDevice, c->st));
   }
-  // back up the state so that tuning leaves the grid unchanged
-  void *bk[2] = {nullptr, nullptr};
+  // back up the state so that tuning leaves the grid unchanged; the backup is
+  // freed on every return, early error returns included
   const size_t fb = (size_t)g.elems * c->tsz;
-  auto free_bk = [&]() {
-    for (void *p : bk)
-      if (p) {
-        cudaFree(p);
-        c->dev_bytes -= (double)fb;
-      }
-  };
-  if ((e = dev_alloc(c, &bk[0], fb)) || (e = dev_alloc(c, &bk[1], fb))) {
-    free_bk();
-    return e;
-  }
+  struct Backup {
+    girih_gpu_ctx *c;
+    size_t fb;
+    void *p[2];
+    ~Backup() {
+      for (void *q : p)
+        if (q) {
+          cudaFree(q);
+          c->dev_bytes -= (double)fb;
+        }
+    }
+  } backup{c, fb, {nullptr, nullptr}};
+  void **bk = backup.p;
+  if ((e = dev_alloc(c, &bk[0], fb)) || (e = dev_alloc(c, &bk[1], fb))) return e;
   CK(cudaMemcpyAsync(bk[0], c->f[c->iu1], fb, cudaMemcpyDeviceToDevice, c->st));
   CK(cudaMemcpyAsync(bk[1], c->f[c->iu2], fb, cudaMemcpyDeviceToDevice, c->st));
   const int steps = trial_steps > 0 ? 2 * ((trial_steps + 1) / 2) : (g.r == 4 ? 8 : 24);
-  const int saved_sched = c->sched;
-  const FusedConfig saved_cfg = c->fcfg;
   double best = 1e300;
   TuneChoice best_c = cands[0];
   drop_graph(c);
@@ -845,10 +846,7 @@ int girih_gpu_autotune(girih_gpu_ctx *c, int trial_steps, girih_gpu_info_t *chos
     for (int rep = 0; rep < 3; rep++) {
       int a = c->iu1, b = c->iu2, launches = 0;
       CK(cudaEventRecord(c->e0, c->st));
-      if ((e = issue_steps(c, steps, &launches, &a, &b))) {
-        free_bk();
-        return e;
-      }
+      if ((e = issue_steps(c, steps, &launches, &a, &b))) return e;
       CK(cudaEventRecord(c->e1, c->st));
       CK(cudaEventSynchronize(c->e1));
       float ms = 0;
@@ -866,11 +864,8 @@ int girih_gpu_autotune(girih_gpu_ctx *c, int trial_steps, girih_gpu_info_t *chos
   CK(cudaMemcpyAsync(c->f[0], bk[0], fb, cudaMemcpyDeviceToDevice, c->st));
   CK(cudaMemcpyAsync(c->f[1], bk[1], fb, cudaMemcpyDeviceToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
-  free_bk();
   c->iu1 = 0;
   c->iu2 = 1;
-  (void)saved_sched;
-  (void)saved_cfg;
   c->sched = best_c.sched;
   c->fcfg = best_c.sched == GIRIH_SCHED_FUSED ? make_fused_config(g, prec, best_c.depth, best_c.variant) : FusedConfig{};
   if (!explicit_cfg) {

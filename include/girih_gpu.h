@@ -166,7 +166,8 @@ int girih_gpu_info(girih_gpu_ctx *c, girih_gpu_info_t *info);
  * default), keeps the fastest and restores the grid state.  Choices are cached
  * per operator, precision and size class (log2 of the point count), and later
  * contexts created with fusion_depth = 0 and no tile pick them up.  *chosen
- * (may be NULL) receives the result. */
+ * (may be NULL) receives the result.  After an error return the grid state is
+ * unspecified (upload again). */
 int girih_gpu_autotune(girih_gpu_ctx *c, int trial_steps, girih_gpu_info_t *chosen);
 
 /* Time-fused stepping without any device allocation.  This entry point has no

@@ -120,6 +120,9 @@ extern "C" int girih_gpu_fused_run_noalloc(const girih_gpu_desc *d, void *U1, vo
                        std::to_string((unsigned long long)GIRIH_NOALLOC_SCRATCH_BYTES) + "-byte scratch");
   FusedConfig cfg = choose_fused_config(g, d->precision, d->fusion_depth, d->block_x, d->block_y);
   if (!cfg.depth) return fail_na(GIRIH_GPU_EUNSUPPORTED, "requested fused tile/depth is not provided");
+  if (cfg.box_w)  // TMA tiles read through tensor maps that a context encodes and keeps per array
+    return fail_na(GIRIH_GPU_EUNSUPPORTED,
+                   "the requested tile is a TMA-staged variant, which only the context entry points run");
 
   int prev_dev = -1;
   cudaGetDevice(&prev_dev);

@@ -305,7 +305,7 @@ class Batch:
 
 
 def fused_run_noalloc(op, nx, ny, nz, U1, U2, U3, coefs, nt, precision="fp64", pnx=None, fusion_depth=0,
-                      device=0, stream=None):
+                      device=0, stream=None, block=(0, 0)):
     """Fused time loop on caller-owned DEVICE arrays (reference layout, raw
     device addresses) without any device allocation by the library."""
     r = OP_INFO[op][0]
@@ -317,6 +317,7 @@ def fused_run_noalloc(op, nx, ny, nz, U1, U2, U3, coefs, nt, precision="fp64", p
     d.precision = PRECISIONS[precision]
     d.schedule = FUSED
     d.fusion_depth = fusion_depth
+    d.block_x, d.block_y = block
     d.device = device
     cc = (ctypes.c_double * 5)(*(list(coefs)[:5] + [0.0] * (5 - len(list(coefs)[:5]))))
     _check(lib().girih_gpu_fused_run_noalloc(ctypes.byref(d), U1, U2, U3, cc, nt, stream),

@@ -178,7 +178,9 @@ int girih_gpu_autotune(girih_gpu_ctx *c, int trial_steps, girih_gpu_info_t *chos
  * can cause.  The caller passes its own device arrays U1, U2 (in/out) and U3
  * (roc2, time-order-2 operators) in the reference layout (ldomain_shape,
  * element type FP64 for GIRIH_FP64, FP32 otherwise) and the r+1 constant
- * coefficients; operators 0, 1 and 8; U1 and U2 must carry equal halos.  The
+ * coefficients; operators 0, 1 and 8; U1 and U2 must carry equal halos; an
+ * explicit tile (block_x, block_y) must not name a TMA-staged variant, whose
+ * tensor maps only a context keeps (GIRIH_GPU_EUNSUPPORTED).  The
  * call advances nt steps like girih_gpu_run() (U1 = state steps-1, U2 = state
  * steps) and returns when the work on `stream` (a cudaStream_t, NULL = default
  * stream) is done.  The two spare state arrays of the fused schedule live in a

@@ -71,3 +71,25 @@ def test_no_device_is_an_error_code():
     with pytest.raises(gpu.GirihGpuError) as e:
         gpu.Context(1, 8, 8, 8)
     assert e.value.code == 7
+
+
+def test_noalloc_validates_before_touching_the_device():
+    """The no-allocation entry point rejects bad requests before any CUDA call
+    (the pointers below are never dereferenced on the host)."""
+    fake = 1 << 20  # 16-byte aligned stand-ins for device addresses
+    coefs = [-0.75, 0.125]
+    cases = [
+        (dict(op=5), 2),                                   # variable coefficients: no fused no-alloc form
+        (dict(op=8, U3=None), 1),                           # time order 2 needs roc2
+        (dict(op=1, nx=300, ny=300, nz=300), 1),            # two FP64 states beyond the static scratch
+        (dict(op=8, precision="mixed", fusion_depth=4, block=(53, 24)), 2),  # a TMA tile
+        (dict(op=1, U1=fake + 8), 1),                       # misaligned array
+    ]
+    for kw, code in cases:
+        args = dict(op=1, nx=20, ny=16, nz=12, U1=fake, U2=fake, U3=fake, coefs=coefs, nt=2)
+        args.update(kw)
+        n = args.pop("nx")
+        with pytest.raises(gpu.GirihGpuError) as e:
+            gpu.fused_run_noalloc(args.pop("op"), n, args.pop("ny"), args.pop("nz"), args.pop("U1"),
+                                  args.pop("U2"), args.pop("U3"), args.pop("coefs"), args.pop("nt"), **args)
+        assert e.value.code == code, (kw, str(e.value))

@@ -177,6 +177,34 @@ __device__ __forceinline__ float leapfrog_compensated(float v, float u, float r2
   return __fadd_rn(s, fmaf(r2, lap, e));
 }
 
+// Packed FP32 pairs: sm_100-class GPUs execute f32x2 add / multiply / FMA as
+// one FMA-pipe instruction for two values, each rounded as its scalar
+// counterpart.  The radius-1 constant-coefficient levels run a thread's
+// columns two at a time with the scalar code's association order (the
+// compiler contracts s + c*p into fma(c, p, s)); a - b is fma(-1, b, a), the
+// same single rounding as __fsub_rn.
+__device__ __forceinline__ float2 f2_sub(float2 a, float2 b) {
+  return __ffma2_rn(make_float2(-1.f, -1.f), b, a);
+}
+
+// star_const_sum<1, FastArith> on two columns: c0 v + c1 x + c1 y + c1 z.
+__device__ __forceinline__ float2 star1_sum2(const float *cc, float2 v, float2 px, float2 py, float2 pz) {
+  const float2 c1 = make_float2(cc[1], cc[1]);
+  float2 s = __fmul2_rn(make_float2(cc[0], cc[0]), v);
+  s = __ffma2_rn(c1, px, s);
+  s = __ffma2_rn(c1, py, s);
+  return __ffma2_rn(c1, pz, s);
+}
+
+// leapfrog_compensated on two columns; -u - bb is -(u + bb), exactly.
+__device__ __forceinline__ float2 leapfrog_compensated2(float2 v, float2 u, float2 r2, float2 lap) {
+  const float2 a = __fadd2_rn(v, v);
+  const float2 s = f2_sub(a, u);
+  const float2 bb = f2_sub(s, a);
+  const float2 e = f2_sub(f2_sub(a, f2_sub(s, bb)), __fadd2_rn(u, bb));
+  return __fadd2_rn(s, __ffma2_rn(r2, lap, e));
+}
+
 __device__ __forceinline__ int pmod(int a, int m) { return ((a % m) + m) % m; }
 
 
@@ -453,6 +481,35 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
             xlp.load(srow - VX);
             xrp.load(srow + VX);
           }
+          // radius-1 constant-coefficient operators in FP32: column pairs in f32x2
+          constexpr bool PAIRS = std::is_same<T, float>::value && R == 1 && !VAR && (OP == 1 || OP == 8) &&
+                                 VX % 2 == 0;
+          if constexpr (PAIRS) {
+            static_for<VX / 2>([&](auto p_c) {
+              constexpr int V0 = 2 * decltype(p_c)::value, V1 = V0 + 1;
+              const FusedAcc<R, T, QL, SL, VX, V0> a0{srow, q[L - 1][c], yv, xlp.e, xrp.e};
+              const FusedAcc<R, T, QL, SL, VX, V1> a1{srow, q[L - 1][c], yv, xlp.e, xrp.e};
+              const float2 v2 = make_float2(a0.c(), a1.c());
+              const float2 lap = star1_sum2(cc, v2, __fadd2_rn(make_float2(a0.x(1), a1.x(1)), make_float2(a0.x(-1), a1.x(-1))),
+                                            __fadd2_rn(make_float2(a0.y(1), a1.y(1)), make_float2(a0.y(-1), a1.y(-1))),
+                                            __fadd2_rn(make_float2(a0.z(1), a1.z(1)), make_float2(a0.z(-1), a1.z(-1))));
+              float2 cand;
+              if constexpr (TO == 2) {
+                float2 uold;
+                if constexpr (L >= 2) uold = make_float2(q[L - 2][c][V0][SL], q[L - 2][c][V1][SL]);
+                else uold = make_float2(pvc[c].e[V0], pvc[c].e[V1]);
+                const float2 r2 = make_float2(r2c[L - 1][c].e[V0], r2c[L - 1][c].e[V1]);
+                if constexpr (COMP) cand = leapfrog_compensated2(v2, uold, r2, lap);
+                else cand = __ffma2_rn(r2, lap, f2_sub(__fadd2_rn(v2, v2), uold));  // (2v - u) + roc2*lap
+              } else {
+                cand = lap;
+              }
+              const bool on0 = p_int && (act >> (((L - 1) * CY + c) * VX + V0) & 1u);
+              const bool on1 = p_int && (act >> (((L - 1) * CY + c) * VX + V1) & 1u);
+              val[V0] = on0 ? cand.x : v2.x;  // halo and out-of-region points keep their value
+              val[V1] = on1 ? cand.y : v2.y;
+            });
+          } else
           static_for<VX>([&](auto v_c) {
             constexpr int V = decltype(v_c)::value;
             const T centre = q[L - 1][c][V][SL];

@@ -19,6 +19,7 @@
 // level below.
 #pragma once
 #include <algorithm>
+#include <atomic>
 #include <type_traits>
 #include <utility>
 
@@ -665,11 +666,16 @@ cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
   if constexpr (TMA) kern = (void *)fused_pass_tma<OP, T, COMP, TT, NTX, NTY, CY, VX>;
   else kern = (void *)fused_pass<OP, T, COMP, TT, NTX, NTY, CY, VX, SRC>;
   const size_t smem = S::smem_bytes;
-  static bool attr_set = false;  // per instantiation, host side
-  if (!attr_set) {
+  // the shared-memory opt-in is a function attribute of each device: set it once
+  // per (instantiation, device), from any host thread
+  static std::atomic<unsigned long long> attr_set{0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const unsigned long long dev_bit = 1ull << (dev & 63);
+  if (!(attr_set.load(std::memory_order_acquire) & dev_bit)) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    attr_set = true;
+    attr_set.fetch_or(dev_bit, std::memory_order_release);
   }
   int occ = 1;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, NTX * NTY, smem);
@@ -677,11 +683,7 @@ cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
   const int gx = (g.nx + BX - 1) / BX, gy = (g.ny + BY - 1) / BY;
   const int64_t tiles = (int64_t)gx * gy;
   int nsm = 152;
-  {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  }
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const int64_t cap = (int64_t)nsm * occ;
   // choose the number of z chunks: minimise waves x (chunk + pipeline overhead)
   const int over = TT * R + TT * (R + 1);

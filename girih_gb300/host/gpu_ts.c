@@ -13,7 +13,8 @@
  * copied to the GPU, the time loop runs there, and U1 (state nt-1) and U2
  * (state nt) are copied back.  The reference CLI has no precision or schedule
  * options, so they come from the environment:
- *   GIRIH_GPU_PRECISION = fp64 (default) | fp32 | mixed
+ *   GIRIH_GPU_PRECISION = fp64 (default) | fp32 | mixed | fp64df (FP64 fields, fused
+ *                         passes in double-float arithmetic)
  *   GIRIH_GPU_SCHEDULE  = plain (default) | fused | auto
  *   GIRIH_GPU_EXACT     = 1 (default for fp64 plain: the serial reference's rounding,
  *                         so --verify 1 passes its bit-exact check) | 0
@@ -72,7 +73,7 @@ static void gpu_ts_fail(Parameters *p, const char *what, int err) {
 
 void gpu_ts(Parameters *p) {
   const double t0 = wall_now();
-  static const char *const precisions[] = {"fp64", "fp32", "mixed"};
+  static const char *const precisions[] = {"fp64", "fp32", "mixed", "fp64df"};  /* GIRIH_FP64 .. GIRIH_FP64_DF */
   static const char *const schedules[] = {"plain", "fused", "auto"};
   if (p->mpi_size != 1) RAISE_ERROR("the GPU time stepper runs one grid per process: use a single rank");
   if (p->stencil.type != REGULAR || p->stencil.shape != STAR)
@@ -86,7 +87,7 @@ void gpu_ts(Parameters *p) {
     d.ldomain_shape[i] = p->ldomain_shape[i];
   }
   d.host_real_size = (int)sizeof(real_t);
-  d.precision = env_choice("GIRIH_GPU_PRECISION", precisions, 3, GIRIH_FP64);
+  d.precision = env_choice("GIRIH_GPU_PRECISION", precisions, 4, GIRIH_FP64);
   d.schedule = env_choice("GIRIH_GPU_SCHEDULE", schedules, 3, GIRIH_SCHED_PLAIN);
   const char *ex = getenv("GIRIH_GPU_EXACT");
   d.exact = ex ? atoi(ex) != 0 : (d.precision == GIRIH_FP64 && d.schedule == GIRIH_SCHED_PLAIN);

@@ -70,6 +70,26 @@ def test_gpu_stepper_host_logic_verifies(driver, oracle_stub, kernel):
     assert "PASSED" in r.stdout
 
 
+@pytest.mark.parametrize("precision,schedule", [("fp64df", "fused"), ("mixed", "auto"), ("fp32", "plain")])
+def test_gpu_stepper_accepts_every_form(driver, oracle_stub, precision, schedule):
+    """Every precision and schedule of the library is selectable from the
+    reference CLI's environment (the oracle stand-in computes exactly, so the
+    reference's bit-exact --verify 1 still passes)."""
+    env = dict(oracle_stub, GIRIH_GPU_PRECISION=precision, GIRIH_GPU_SCHEDULE=schedule)
+    r = subprocess.run([driver, "--nx", "18", "--ny", "12", "--nz", "10", "--nt", "4", "--target-kernel", "1",
+                        "--target-ts", "3", "--verify", "1"], capture_output=True, text=True, env=env)
+    assert r.returncode == 0, r.stderr
+    assert "PASSED" in r.stdout
+
+
+def test_gpu_stepper_rejects_unknown_precision(driver, oracle_stub):
+    env = dict(oracle_stub, GIRIH_GPU_PRECISION="fp16")
+    r = subprocess.run([driver, "--nx", "8", "--ny", "8", "--nz", "8", "--nt", "2", "--target-kernel", "1",
+                        "--target-ts", "3"], capture_output=True, text=True, env=env)
+    assert r.returncode == 1
+    assert "GIRIH_GPU_PRECISION=fp16" in r.stderr
+
+
 def _parse_py_summary(text):
     """The key matching of the reference's scripts/parse.py get_summary():
     a line starting with '<field>:' gives the first token after the colon."""

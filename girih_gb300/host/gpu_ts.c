@@ -19,6 +19,14 @@
  *   GIRIH_GPU_EXACT     = 1 (default for fp64 plain: the serial reference's rounding,
  *                         so --verify 1 passes its bit-exact check) | 0
  *   GIRIH_GPU_DEVICE    = CUDA device ordinal (default 0)
+ *   GIRIH_GPU_AUTOTUNE  = 1: time the tile shapes and fusion depths on this grid
+ *                         (girih_gpu_autotune, the counterpart of the MWD
+ *                         auto-tuner, src/kernels/diamond_utils.c:691-847) when
+ *                         the stepper first sees a grid; the state is restored,
+ *                         but that first call's time includes the tuning
+ * The MWD option --t-dim (diamond time unroll, default -1 = tune) sets the
+ * fusion depth of the fused schedule to t_dim + 1 time steps per pass (clamped
+ * to the deepest pass provided for the operator and precision).
  * Errors are reported through the reference's RAISE_ERROR.
  *
  * gpu_ts_report() prints the run's rates in the key format of the reference's
@@ -93,18 +101,30 @@ void gpu_ts(Parameters *p) {
   d.exact = ex ? atoi(ex) != 0 : (d.precision == GIRIH_FP64 && d.schedule == GIRIH_SCHED_PLAIN);
   const char *dev = getenv("GIRIH_GPU_DEVICE");
   d.device = dev ? atoi(dev) : 0;
+  if (p->t_dim >= 0) d.fusion_depth = p->t_dim + 1;
+  const char *tune = getenv("GIRIH_GPU_AUTOTUNE");
+  const int autotune = tune && atoi(tune) != 0;
 
   if (g_ctx && memcmp(&d, &g_desc, sizeof(d)) != 0) gpu_ts_release();
-  int e;
+  int e, fresh = 0;
   if (!g_ctx) {
     if ((e = girih_gpu_create(&g_ctx, &d))) {
       g_ctx = NULL;
       gpu_ts_fail(p, "girih_gpu_create", e);
     }
     g_desc = d;
+    fresh = 1;
     atexit(gpu_ts_release);
   }
   if ((e = girih_gpu_upload(g_ctx, p->U1, p->U2, p->U3, p->coef))) gpu_ts_fail(p, "girih_gpu_upload", e);
+  if (fresh && autotune) {
+    girih_gpu_info_t tuned;
+    if ((e = girih_gpu_autotune(g_ctx, 0, &tuned))) gpu_ts_fail(p, "girih_gpu_autotune", e);
+    if (p->verbose && p->mpi_rank == 0)
+      printf("GPU stepper autotune: %s schedule, depth %d, tile %d x %d\n",
+             tuned.schedule == GIRIH_SCHED_PLAIN ? "plain" : "fused", tuned.fusion_depth, tuned.block_x,
+             tuned.block_y);
+  }
   /* the reference's source-point update (nb_naive_ts.c:190,196), when switched on */
   if (p->source_point_enabled == 1 && p->has_source == 1 && p->source && p->nt > 0) {
     double *src = (double *)malloc(sizeof(double) * (size_t)p->nt);

@@ -109,8 +109,18 @@ int girih_gpu_info(girih_gpu_ctx *c, girih_gpu_info_t *info) {
   memset(info, 0, sizeof(*info));
   info->precision = c->d.precision;
   info->schedule = c->d.schedule;
+  info->fusion_depth = c->d.fusion_depth > 0 ? c->d.fusion_depth : 1;
   strcpy(info->kernel_name, "oracle stand-in");
   return GIRIH_GPU_OK;
+}
+
+/* The tuner only chooses among schedules that give the same steps; the
+ * stand-in has one, so tuning leaves everything as it is. */
+int girih_gpu_autotune(girih_gpu_ctx *c, int trial_steps, girih_gpu_info_t *chosen) {
+  (void)trial_steps;
+  if (!c) return GIRIH_GPU_EINVAL;
+  if (!c->uploaded) return GIRIH_GPU_ESTATE;
+  return chosen ? girih_gpu_info(c, chosen) : GIRIH_GPU_OK;
 }
 
 const char *girih_gpu_strerror(int err) { return err ? "error (oracle stand-in)" : "ok"; }

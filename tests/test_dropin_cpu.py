@@ -82,6 +82,18 @@ def test_gpu_stepper_accepts_every_form(driver, oracle_stub, precision, schedule
     assert "PASSED" in r.stdout
 
 
+def test_gpu_stepper_t_dim_sets_fusion_depth_and_autotune(driver, oracle_stub):
+    """--t-dim (the MWD time unroll) becomes the fusion depth t_dim + 1;
+    GIRIH_GPU_AUTOTUNE=1 tunes when the stepper first sees the grid."""
+    env = dict(oracle_stub, GIRIH_GPU_SCHEDULE="fused", GIRIH_GPU_PRECISION="mixed", GIRIH_GPU_AUTOTUNE="1")
+    r = subprocess.run([driver, "--nx", "18", "--ny", "12", "--nz", "10", "--nt", "4", "--target-kernel", "1",
+                        "--target-ts", "3", "--t-dim", "3", "--verify", "1"], capture_output=True, text=True, env=env)
+    assert r.returncode == 0, r.stderr
+    assert "PASSED" in r.stdout
+    assert "GPU stepper autotune: fused schedule, depth 4" in r.stdout
+    assert "mixed fused depth 4" in r.stdout
+
+
 def test_gpu_stepper_rejects_unknown_precision(driver, oracle_stub):
     env = dict(oracle_stub, GIRIH_GPU_PRECISION="fp16")
     r = subprocess.run([driver, "--nx", "8", "--ny", "8", "--nz", "8", "--nt", "2", "--target-kernel", "1",

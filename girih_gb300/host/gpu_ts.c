@@ -44,6 +44,8 @@
 
 static girih_gpu_ctx *g_ctx = NULL;
 static girih_gpu_desc g_desc;
+static const char *const precisions[] = {"fp64", "fp32", "mixed", "fp64df"};  /* GIRIH_FP64 .. GIRIH_FP64_DF */
+static const char *const schedules[] = {"plain", "fused", "auto"};
 
 /* per-call wall time (the span the reference's MPI_Wtime bracket measures,
  * src/performance.c:74-78) and device time, over all calls */
@@ -81,8 +83,6 @@ static void gpu_ts_fail(Parameters *p, const char *what, int err) {
 
 void gpu_ts(Parameters *p) {
   const double t0 = wall_now();
-  static const char *const precisions[] = {"fp64", "fp32", "mixed", "fp64df"};  /* GIRIH_FP64 .. GIRIH_FP64_DF */
-  static const char *const schedules[] = {"plain", "fused", "auto"};
   if (p->mpi_size != 1) RAISE_ERROR("the GPU time stepper runs one grid per process: use a single rank");
   if (p->stencil.type != REGULAR || p->stencil.shape != STAR)
     RAISE_ERROR("the GPU time stepper provides the star operators only");
@@ -161,7 +161,9 @@ void gpu_ts(Parameters *p) {
 
 /* Rates of the calls so far in scripts/parse.py's keys (MStencil/s per time
  * step: ln_stencils * nt / time, the reference's GStencil/s x 1000), plus the
- * device-only rate of the fastest call. */
+ * device-only rate of the fastest call, then one machine-readable line (prefix
+ * "GPU stepper JSON: ") with the form the library ran, its compulsory bytes
+ * per lattice update and the algorithmic HBM rate they imply. */
 void gpu_ts_report(const Parameters *p) {
   if (p->mpi_rank != 0 || g_stats.calls == 0) return;
   const double per_step = (double)p->ln_stencils * p->nt / 1e6;
@@ -169,4 +171,17 @@ void gpu_ts_report(const Parameters *p) {
   printf("RANK0 MStencil/s  AVG: %f\n", per_step / (g_stats.wall_sum / g_stats.calls));
   printf("RANK0 MStencil/s  MAX: %f\n", per_step / g_stats.wall_min);
   if (g_stats.dev_min > 0) printf("GPU device MStencil/s MAX: %f\n", per_step / g_stats.dev_min);
+  girih_gpu_info_t info;
+  if (!g_ctx || girih_gpu_info(g_ctx, &info) != 0) return;
+  const double glups_wall = per_step / g_stats.wall_min / 1e3;
+  const double glups_dev = g_stats.dev_min > 0 ? per_step / g_stats.dev_min / 1e3 : 0.0;
+  const int prec = info.precision >= 0 && info.precision <= GIRIH_FP64_DF ? info.precision : 0;
+  const int sched = info.schedule >= 0 && info.schedule <= GIRIH_SCHED_AUTO ? info.schedule : 0;
+  printf("GPU stepper JSON: {\"stepper\": \"GPU (libgirih_gpu)\", \"target_kernel\": %d, "
+         "\"grid\": [%d, %d, %d], \"nt\": %d, \"calls\": %d, \"precision\": \"%s\", \"schedule\": \"%s\", "
+         "\"fusion_depth\": %d, \"tile\": [%d, %d], \"kernel\": \"%s\", \"bytes_per_lup\": %.1f, "
+         "\"glups_wall_max\": %.6g, \"glups_device_max\": %.6g, \"algorithmic_gbs_device\": %.6g}\n",
+         p->target_kernel, p->lstencil_shape[0], p->lstencil_shape[1], p->lstencil_shape[2], p->nt, g_stats.calls,
+         precisions[prec], schedules[sched], info.fusion_depth, info.block_x, info.block_y, info.kernel_name,
+         info.bytes_per_lup, glups_wall, glups_dev, glups_dev * info.bytes_per_lup);
 }

@@ -110,6 +110,7 @@ int girih_gpu_info(girih_gpu_ctx *c, girih_gpu_info_t *info) {
   info->precision = c->d.precision;
   info->schedule = c->d.schedule;
   info->fusion_depth = c->d.fusion_depth > 0 ? c->d.fusion_depth : 1;
+  info->bytes_per_lup = 8.0 * (2 + (c->to == 2 ? 2 : 0) + (c->arr ? c->nc : 0));  /* FP64, one step per pass */
   strcpy(info->kernel_name, "oracle stand-in");
   return GIRIH_GPU_OK;
 }

@@ -133,3 +133,10 @@ def test_gpu_stepper_report_has_parse_py_keys(driver, oracle_stub):
     assert m["Number of time steps"] == 4 and m["Number of tests"] == 3
     assert 0 < m["RANK0 MStencil/s  MIN"] <= m["RANK0 MStencil/s  AVG"] * 1.0001 <= m["RANK0 MStencil/s  MAX"] * 1.0002
     assert "GPU device MStencil/s MAX:" in r.stdout
+    import json
+    js = [ln.split("GPU stepper JSON: ", 1)[1] for ln in r.stdout.splitlines() if ln.startswith("GPU stepper JSON: ")]
+    assert len(js) == 1
+    d = json.loads(js[0])
+    assert d["target_kernel"] == 1 and d["grid"] == [24, 24, 24] and d["nt"] == 4 and d["calls"] == 3
+    assert d["precision"] == "fp64" and d["schedule"] == "plain" and d["bytes_per_lup"] == 16.0
+    assert d["glups_device_max"] > 0 and d["algorithmic_gbs_device"] == pytest.approx(16.0 * d["glups_device_max"], rel=1e-3)

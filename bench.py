@@ -434,8 +434,8 @@ def run_reference(args, wl, rank, world):
     if rank != 0:
         return None
     vals = []
-    for _ in range(args.warmup):
-        pass  # the CPU restatement has no warm-up state beyond its first sweeps
+    # no warm-up runs: each step's sample times its own sweeps after one untimed pair
+    # (cpu_baseline), which is the only state the CPU restatement warms
     threads = os.cpu_count() or 1
     per_step_s = max(1.0, args.cpu_seconds / max(1, args.steps))
     cb = None

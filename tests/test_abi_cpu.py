@@ -93,3 +93,30 @@ def test_noalloc_validates_before_touching_the_device():
             gpu.fused_run_noalloc(args.pop("op"), n, args.pop("ny"), args.pop("nz"), args.pop("U1"),
                                   args.pop("U2"), args.pop("U3"), args.pop("coefs"), args.pop("nt"), **args)
         assert e.value.code == code, (kw, str(e.value))
+
+
+def test_ctypes_structs_match_the_header_layout(tmp_path):
+    """The Python binding's girih_gpu_desc / girih_gpu_info_t mirror the C
+    header field by field (offsets and sizes from the C compiler)."""
+    src = tmp_path / "layout.c"
+    fields = {"girih_gpu_desc": [f for f, _ in gpu.Desc._fields_], "girih_gpu_info_t": [f for f, _ in gpu.Info._fields_]}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "girih_gpu.h"', "int main(void) {"]
+    for st, names in fields.items():
+        lines.append(f'  printf("{st} size %zu\\n", sizeof({st}));')
+        for n in names:
+            lines.append(f'  printf("{st} {n} %zu\\n", offsetof({st}, {n}));')
+    lines += ["  return 0;", "}"]
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {tuple(ln.split()[:2]): int(ln.split()[2]) for ln in out if ln}
+    for st, cls in (("girih_gpu_desc", gpu.Desc), ("girih_gpu_info_t", gpu.Info)):
+        assert got[(st, "size")] == ctypes.sizeof(cls), st
+        for n in fields[st]:
+            assert got[(st, n)] == getattr(cls, n).offset, (st, n)
+
+
+def test_binding_and_oracle_agree_on_operators():
+    import oracle
+    assert gpu.OP_INFO == {k: (r, to, nc, bool(arr)) for k, (r, to, nc, arr) in oracle.OP_INFO.items()}

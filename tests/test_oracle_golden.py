@@ -120,3 +120,24 @@ def test_oracle_source_rejects_halo_point():
     g, s = _grid_for("k1_src")
     with pytest.raises(ValueError):
         g.run_source(2, (0, 5, 5), [1.0, 2.0])
+
+
+_HARNESS = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref", "ref_golden")
+
+
+@pytest.mark.skipif(not os.path.exists(_HARNESS), reason="reference harness not built (needs the reference sources)")
+@pytest.mark.parametrize("name", ["k0_seed", "k1_ref_odd_nt", "k4_ref", "k5_src"])
+def test_fixtures_are_what_the_reference_produces(name):
+    """Re-running the reference's own stepper reproduces the committed fixture
+    bit for bit (the fixtures are the reference's output, not the oracle's)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "make_golden", os.path.join(os.path.dirname(__file__), "golden", "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    cases = {c[0]: (c, False) for c in mg.CASES}
+    cases.update({c[0]: (c, True) for c in mg.SOURCE_CASES})
+    (_, op, nx, ny, nz, nt, init, sp), source = cases[name]
+    u1, u2, _ = mg.run_case(op, nx, ny, nz, nt, init, sp, source)
+    np.testing.assert_array_equal(u1, _data[name + "__U1"])
+    np.testing.assert_array_equal(u2, _data[name + "__U2"])

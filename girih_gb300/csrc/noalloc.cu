@@ -13,8 +13,10 @@
 // every GPU that loads this library holds it until the process exits.  All
 // calls share it and it keeps the last call's contents, so calls whose work
 // overlaps on the GPU (different streams, different host threads) race on it:
-// serialise them.  Each call re-initialises what it reads (both spare buffers
-// are overwritten from U2 before the first pass).
+// serialise them.  Each call re-initialises what it reads (the halo flag is
+// cleared and both spare buffers are overwritten from U2 before the first
+// pass).  The first call in a device context looks up the array's device
+// address (set-up); later calls in the same context reuse it.
 #include <mutex>
 #include <string>
 
@@ -30,22 +32,61 @@ constexpr size_t kFlagBytes = 256;  // halo-equality flag, then the two spare bu
 constexpr int kMaxDevices = 64;
 
 std::mutex g_setup_mutex;
-void *g_scratch_addr[kMaxDevices] = {};
+struct ScratchSlot {
+  void *addr;
+  unsigned long long ctx_id;  // device context the address belongs to
+};
+ScratchSlot g_scratch[kMaxDevices] = {};
 
-// Device address of the scratch array on the current device, looked up once
-// per device.  In host code the array's name is only a host-side stand-in.
+// Unique id of the calling thread's current device context (driver API
+// cuCtxGetCurrent / cuCtxGetId through the runtime's entry-point query, so the
+// library needs no link against libcuda); 0 where unavailable.
+unsigned long long current_context_id() {
+  using GetCurrent = int (*)(void **);
+  using GetId = int (*)(void *, unsigned long long *);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(p);
+  });
+  void *ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&ctx) == 0 && ctx && get_id(ctx, &id) == 0) return id;
+  return 0;
+}
+
+// Device address of the scratch array on the current device (which must be
+// `dev`).  In host code the array's name is only a host-side stand-in, so the
+// address comes from cudaGetSymbolAddress, looked up once per device context:
+// again after a cudaDeviceReset(), which reloads the module and may move the
+// array, and on every call where the context id cannot be read.
 int scratch_address(int dev, unsigned char **out) {
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_addr[dev]) {
+  // (a context not yet bound reads as id 0: the lookup below binds it, and the
+  // next call records its id)
+  const unsigned long long ctx = current_context_id();
+  ScratchSlot &slot = g_scratch[dev];
+  if (!slot.addr || ctx == 0 || slot.ctx_id != ctx) {
     void *p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) {
+      slot.addr = nullptr;
       set_error(std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
       return GIRIH_GPU_ECUDA;
     }
-    g_scratch_addr[dev] = p;
+    slot.addr = p;
+    slot.ctx_id = ctx;
   }
-  *out = static_cast<unsigned char *>(g_scratch_addr[dev]);
+  *out = static_cast<unsigned char *>(slot.addr);
   return 0;
 }
 
@@ -179,14 +220,17 @@ extern "C" int girih_gpu_fused_run_noalloc(const girih_gpu_desc *d, void *U1, vo
     iu2 = spare[1];
     left -= T;
   }
-  // move the final states (U1 = state steps-1, U2 = state steps) back into the caller's arrays
-  if (iu2 == 0) {  // current state sits in U1's array: park it in a spare first
-    const int park = iu1 == 2 ? 3 : 2;
-    NA_CK(cudaMemcpyAsync(buf[park], buf[iu2], state_bytes, cudaMemcpyDeviceToDevice, st));
-    iu2 = park;
+  // The passes alternate between the buffer pairs (0, 1) and (2, 3), so the
+  // final states (U1 = state steps-1, U2 = state steps) are either already in
+  // the caller's arrays (even pass count) or in the two spare buffers (odd).
+  // In the latter case copy them back row by row: nnx columns per row, so the
+  // caller's x padding [nnx, ldomain_shape[0]) keeps its own values (the
+  // spares' padding came from U2).
+  if (iu1 != 0) {
+    const size_t row = (size_t)g.nnx * tsz, pitch = (size_t)g.hpx * tsz, rows = (size_t)g.nny * g.nnz;
+    NA_CK(cudaMemcpy2DAsync(U1, pitch, buf[iu1], pitch, row, rows, cudaMemcpyDeviceToDevice, st));
+    NA_CK(cudaMemcpy2DAsync(U2, pitch, buf[iu2], pitch, row, rows, cudaMemcpyDeviceToDevice, st));
   }
-  if (iu1 != 0) NA_CK(cudaMemcpyAsync(buf[0], buf[iu1], state_bytes, cudaMemcpyDeviceToDevice, st));
-  if (iu2 != 1) NA_CK(cudaMemcpyAsync(buf[1], buf[iu2], state_bytes, cudaMemcpyDeviceToDevice, st));
   NA_CK(cudaStreamSynchronize(st));
   NA_CK(cudaGetLastError());
   return 0;

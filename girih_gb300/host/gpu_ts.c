@@ -84,8 +84,10 @@ static void gpu_ts_fail(Parameters *p, const char *what, int err) {
 void gpu_ts(Parameters *p) {
   const double t0 = wall_now();
   if (p->mpi_size != 1) RAISE_ERROR("the GPU time stepper runs one grid per process: use a single rank");
-  if (p->stencil.type != REGULAR || p->stencil.shape != STAR)
-    RAISE_ERROR("the GPU time stepper provides the star operators only");
+  /* the regular operators: the star ones and the 27-point box (kernel 7); the
+   * solar kernel (SOLAR type) is not provided */
+  if (p->stencil.type != REGULAR || (p->stencil.shape != STAR && p->stencil.shape != BOX))
+    RAISE_ERROR("the GPU time stepper provides the star and box operators only");
 
   girih_gpu_desc d;
   memset(&d, 0, sizeof(d));

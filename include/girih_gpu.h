@@ -182,14 +182,17 @@ int girih_gpu_autotune(girih_gpu_ctx *c, int trial_steps, girih_gpu_info_t *chos
  * explicit tile (block_x, block_y) must not name a TMA-staged variant, whose
  * tensor maps only a context keeps (GIRIH_GPU_EUNSUPPORTED).  The
  * call advances nt steps like girih_gpu_run() (U1 = state steps-1, U2 = state
- * steps) and returns when the work on `stream` (a cudaStream_t, NULL = default
- * stream) is done.  The two spare state arrays of the fused schedule live in a
- * static device array of GIRIH_NOALLOC_SCRATCH_BYTES that every GPU loading
- * this library holds until the process exits: grids whose two state arrays do
- * not fit are rejected with GIRIH_GPU_EINVAL.  All calls share that array, so
- * calls that overlap on the GPU race; serialise them.  The first call on a
- * device looks up the array's device address, so make it before any stream
- * capture. */
+ * steps; halos and x padding of the caller's arrays keep their values) and
+ * waits for its work on `stream` (a cudaStream_t, NULL = default stream) to
+ * finish before it returns.  The two spare state arrays of the fused schedule
+ * live in a static device array of GIRIH_NOALLOC_SCRATCH_BYTES that every GPU
+ * loading this library holds until the process exits: grids whose two state
+ * arrays do not fit are rejected with GIRIH_GPU_EINVAL.  All calls share that
+ * array and it keeps the last call's contents (each call re-initialises what
+ * it reads), so calls that overlap on the GPU race: serialise them.  The first
+ * call in a device context (and the first after a cudaDeviceReset()) does a
+ * one-time set-up, looking up the array's device address; make that first
+ * call before any stream capture begins. */
 #define GIRIH_NOALLOC_SCRATCH_BYTES (64u << 20)
 int girih_gpu_fused_run_noalloc(const girih_gpu_desc *d, void *U1, void *U2, const void *U3,
                                 const double *coefs, int nt, void *stream);

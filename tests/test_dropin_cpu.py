@@ -1,22 +1,26 @@
 """The reference-side drop-in (girih_gb300/host): the girih driver built from
 the reference's own objects with the GPU stepper as --target-ts 3.  Needs the
-reference tree to build, so it runs where that tree exists; without a GPU the
-stepper must fail with a clear error code, never crash."""
+reference sources to build (the tree GIRIH_REF names, or the copy staged in
+baseline/_ref/girih), so it runs where they exist; without a GPU the stepper
+must fail with a clear error code, never crash."""
 import os
 import subprocess
 
 import pytest
 
+from __graft_entry__ import reference_tree
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 EXE = os.path.join(ROOT, "girih_gb300", "host", "_build", "mwd_kernel_gpu")
-REF = "/root/reference"
+REF = reference_tree()
 
-pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src")), reason="reference tree not present")
+pytestmark = pytest.mark.skipif(REF is None, reason="reference sources not present")
 
 
 @pytest.fixture(scope="module")
 def driver():
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={REF}"], check=True)
+    jobs = f"-j{min(16, os.cpu_count() or 4)}"
+    subprocess.run(["make", "-s", jobs, "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={REF}"], check=True)
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "girih_gb300", "host"), f"REF={REF}"], check=True)
     return EXE
 
@@ -60,7 +64,7 @@ def oracle_stub(tmp_path_factory, driver):
     return dict(os.environ, LD_LIBRARY_PATH=str(d), OMP_NUM_THREADS="2")
 
 
-@pytest.mark.parametrize("kernel", ["1", "0", "5"])
+@pytest.mark.parametrize("kernel", ["1", "0", "5", "7"])
 def test_gpu_stepper_host_logic_verifies(driver, oracle_stub, kernel):
     """gpu_ts.c end to end (shapes, upload, run, download) against the
     reference's own --verify 1 bit-exact check, the device replaced by the oracle."""

@@ -93,4 +93,51 @@ __device__ __forceinline__ Df64 df_split(double d, unsigned &range_bad) {
 
 __device__ __forceinline__ double df_to_double(Df64 x) { return (double)x.hi + (double)x.lo; }
 
+// Two double-float values (two neighbouring x columns) with their high and
+// low parts packed as FP32 pairs: the operators above, each instruction a
+// packed f32x2 one (sm_100-class GPUs execute f32x2 add / multiply / FMA as one
+// FMA-pipe instruction for two values, each rounded as its scalar counterpart),
+// so every lane computes exactly what the scalar Df64 code computes.  a - b is
+// fma(-1, b, a): the same single rounding as a scalar subtraction.
+struct Df2 {
+  float2 hi, lo;
+};
+
+__device__ __forceinline__ float2 f2m1() { return make_float2(-1.f, -1.f); }
+__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) { return __ffma2_rn(f2m1(), b, a); }
+
+__device__ __forceinline__ Df2 df2(Df64 a, Df64 b) { return Df2{make_float2(a.hi, b.hi), make_float2(a.lo, b.lo)}; }
+__device__ __forceinline__ Df64 df2_x(const Df2 &a) { return Df64(a.hi.x, a.lo.x); }
+__device__ __forceinline__ Df64 df2_y(const Df2 &a) { return Df64(a.hi.y, a.lo.y); }
+
+__device__ __forceinline__ Df2 operator+(Df2 a, Df2 b) {
+  const float2 s = f2add(a.hi, b.hi);
+  const float2 bb = f2sub(s, a.hi);
+  const float2 e = f2add(f2sub(a.hi, f2sub(s, bb)), f2sub(b.hi, bb));
+  return Df2{s, f2add(e, f2add(a.lo, b.lo))};
+}
+
+__device__ __forceinline__ Df2 operator-(Df2 a, Df2 b) {
+  const float2 s = f2sub(a.hi, b.hi);  // TwoSum of a.hi and -b.hi
+  const float2 bb = f2sub(s, a.hi);
+  const float2 e = f2sub(f2sub(a.hi, f2sub(s, bb)), f2add(b.hi, bb));  // (a - (s - bb)) + (-b - bb)
+  return Df2{s, f2add(e, f2sub(a.lo, b.lo))};
+}
+
+__device__ __forceinline__ Df2 twice(Df2 a) { return Df2{f2add(a.hi, a.hi), f2add(a.lo, a.lo)}; }  // exact
+
+__device__ __forceinline__ Df2 operator*(Df2 a, Df2 b) {
+  const float2 p = __fmul2_rn(a.hi, b.hi);
+  float2 e = __ffma2_rn(a.hi, b.hi, __fmul2_rn(f2m1(), p));  // exact error of the product
+  e = __ffma2_rn(a.hi, b.lo, e);
+  e = __ffma2_rn(a.lo, b.hi, e);
+  return Df2{p, e};
+}
+
+__device__ __forceinline__ Df2 df_norm(Df2 a) {
+  const float2 s = f2add(a.hi, a.lo);
+  return Df2{s, f2sub(a.lo, f2sub(s, a.hi))};
+}
+
 }  // namespace girih

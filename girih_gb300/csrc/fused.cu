@@ -8,7 +8,7 @@ namespace girih {
 bool fused_supported(const Geom &g, int precision) {
   // the fused kernels index with 32-bit element offsets
   if (g.elems >= ((int64_t)1 << 31)) return false;
-  if (g.op == 0 || g.op == 1 || g.op == 8) return true;
+  if (g.op == 0 || g.op == 1 || g.op == 7 || g.op == 8) return true;
   // variable coefficients: FP32 fields (FP32 or BF16 coefficients); their FP64
   // form is bound by the FP64 pipe, where fusion cannot help
   return (g.op >= 2 && g.op <= 5) && (precision == GIRIH_FP32 || precision == GIRIH_MIXED);
@@ -57,11 +57,27 @@ int fused_tile_width(int ntx, int h, int align, bool general_only) {
   return !general_only && aligned >= general ? aligned : general;
 }
 
+// The box operator's own kernel (fused_box.cu): variant 0 = 32 x 32 region
+// (32x16 threads, two rows each), variant 1 = 64 x 16 (64x16 threads, one row);
+// one column per thread, a halo of one column per level.
+static FusedConfig make_box_config(int precision, int depth, int variant) {
+  FusedConfig c{};
+  if (variant > 1 || (precision == GIRIH_FP64_DF && variant == 1 && depth > 2)) return c;
+  const int ntx = variant == 0 ? 32 : 64, ry = variant == 0 ? 32 : 16;
+  c.depth = depth;
+  c.variant = variant;
+  c.bx = ntx - 2 * depth;
+  c.by = ry - 2 * depth;
+  if (c.bx <= 0 || c.by <= 0) c.depth = 0;
+  return c;
+}
+
 FusedConfig make_fused_config(const Geom &g, int precision, int depth, int variant) {
   FusedConfig c{};
   if (!fused_supported(g, precision) || depth < 1 || depth > fused_max_depth(g, precision) ||
       variant < 0 || variant >= FV_COUNT)
     return c;
+  if (g.op == 7) return make_box_config(precision, depth, variant);
   int ntx, ry, vx;
   variant_shape(variant, g.r, precision, &ntx, &ry, &vx);
   if (variant == 2 && precision != GIRIH_FP64_DF && ((g.r == 1 && depth == 4) || (g.r == 4 && depth == 1)))
@@ -118,6 +134,7 @@ cudaError_t launch_fused(const Geom &g, int tsz, int precision, const FusedConfi
       case 1: return launch_fused_op<1, Df64, false>(g, cfg, L, s);
       case 8: return launch_fused_op<8, Df64, false>(g, cfg, L, s);
       case 0: return launch_fused_op<0, Df64, false>(g, cfg, L, s);
+      case 7: return launch_fused_op<7, Df64, false>(g, cfg, L, s);
     }
     return cudaErrorInvalidValue;
   }
@@ -130,6 +147,9 @@ cudaError_t launch_fused(const Geom &g, int tsz, int precision, const FusedConfi
     case 1:
       return tsz == 8 ? launch_fused_op<1, double, false>(g, cfg, L, s)
                       : launch_fused_op<1, float, false>(g, cfg, L, s);
+    case 7:
+      return tsz == 8 ? launch_fused_op<7, double, false>(g, cfg, L, s)
+                      : launch_fused_op<7, float, false>(g, cfg, L, s);
     case 8:
       if (tsz == 8) return launch_fused_op<8, double, false>(g, cfg, L, s);
       return comp ? launch_fused_op<8, float, true>(g, cfg, L, s) : launch_fused_op<8, float, false>(g, cfg, L, s);
@@ -140,6 +160,6 @@ cudaError_t launch_fused(const Geom &g, int tsz, int precision, const FusedConfi
   return cudaErrorInvalidValue;
 }
 
-const char *fused_kernel_name() { return "fused_pass"; }
+const char *fused_kernel_name(int op) { return op == 7 ? "fused_box_pass" : "fused_pass"; }
 
 }  // namespace girih

@@ -58,7 +58,7 @@ FusedConfig make_fused_config(const Geom &g, int precision, int depth, int varia
 FusedConfig choose_fused_config(const Geom &g, int precision, int depth, int bx, int by);
 cudaError_t launch_fused(const Geom &g, int tsz, int precision, const FusedConfig &cfg,
                          const FusedLaunch &L, cudaStream_t s);
-const char *fused_kernel_name();
+const char *fused_kernel_name(int op);
 
 // per-(op, type) launchers defined in the fused_*.cu instantiation files
 template <int OP, class T, bool COMP>
@@ -69,6 +69,8 @@ cudaError_t launch_fused_op(const Geom &g, const FusedConfig &cfg, const FusedLa
                                            cudaStream_t);
 GIRIH_FUSED_SPEC(1, double, false)
 GIRIH_FUSED_SPEC(1, float, false)
+GIRIH_FUSED_SPEC(7, double, false)
+GIRIH_FUSED_SPEC(7, float, false)
 GIRIH_FUSED_SPEC(8, double, false)
 GIRIH_FUSED_SPEC(8, float, false)
 GIRIH_FUSED_SPEC(8, float, true)
@@ -87,6 +89,7 @@ struct Df64;
 GIRIH_FUSED_SPEC(1, Df64, false)
 GIRIH_FUSED_SPEC(8, Df64, false)
 GIRIH_FUSED_SPEC(0, Df64, false)
+GIRIH_FUSED_SPEC(7, Df64, false)
 #undef GIRIH_FUSED_SPEC
 
 }  // namespace girih

@@ -143,20 +143,37 @@ template <class T, int VX> struct Pack {
 // at radius 1 the two scalar loads measured faster.
 __host__ __device__ constexpr bool fused_x_groups(int r, int vx) { return r > 1 && r <= vx; }
 
-template <int R, class T, int QL, int BASE, int VX, int V> struct FusedAcc {
+// XE (radius 1): the two x neighbours across the group's edges come from xe[0]
+// (left) and xe[1] (right), taken from the neighbouring lanes' registers by warp
+// shuffles, instead of from the shared-memory row.
+template <int R, class T, int QL, int BASE, int VX, int V, bool XE = false> struct FusedAcc {
   const T *__restrict__ srow;             // shared-memory row of level l-1 at this thread's first column
   const T (&q)[VX][QL];                   // z queues of the thread's columns (level l-1)
   const T (&yv)[2 * R][VX];               // y neighbours: [d-1] = +d, [R+d-1] = -d
   const T (&xl)[VX], (&xr)[VX];           // fused_x_groups: the x groups left and right of this one
+  const T *xe = nullptr;                  // XE: {left, right} neighbours across the group's edges
+  static_assert(!XE || R == 1, "edge shuffles serve radius-1 operators");
   __device__ __forceinline__ T c() const { return q[V][qslot<QL>(BASE)]; }
   __device__ __forceinline__ T x(int d) const {
     const int pos = V + d;
     if (pos >= 0 && pos < VX) return q[pos < 0 ? 0 : (pos >= VX ? VX - 1 : pos)][qslot<QL>(BASE)];
-    if constexpr (fused_x_groups(R, VX)) return pos < 0 ? xl[pos < -VX ? 0 : pos + VX] : xr[pos >= 2 * VX ? VX - 1 : pos - VX];
+    if constexpr (XE) return pos < 0 ? xe[0] : xe[1];
+    else if constexpr (fused_x_groups(R, VX)) return pos < 0 ? xl[pos < -VX ? 0 : pos + VX] : xr[pos >= 2 * VX ? VX - 1 : pos - VX];
     else return srow[pos];
   }
   __device__ __forceinline__ T y(int d) const { return d > 0 ? yv[d - 1][V] : yv[R - d - 1][V]; }
   __device__ __forceinline__ T z(int d) const { return q[V][qslot<QL>(BASE + d)]; }
+};
+
+// The accessors of two neighbouring double-float columns as one, returning
+// their values as packed pairs (Df2).
+template <class A0, class A1> struct PairAcc {
+  const A0 &a0;
+  const A1 &a1;
+  __device__ __forceinline__ Df2 c() const { return df2(a0.c(), a1.c()); }
+  __device__ __forceinline__ Df2 x(int d) const { return df2(a0.x(d), a1.x(d)); }
+  __device__ __forceinline__ Df2 y(int d) const { return df2(a0.y(d), a1.y(d)); }
+  __device__ __forceinline__ Df2 z(int d) const { return df2(a0.z(d), a1.z(d)); }
 };
 
 template <class F, int... I>
@@ -319,6 +336,12 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
   T cc[5];
 #pragma unroll
   for (int m = 0; m < 5; m++) cc[m] = coef_arg<T>(a, m);
+  // the same coefficients as packed pairs, for the double-float column pairs
+  [[maybe_unused]] Df2 cc2[5];
+  if constexpr (std::is_same<T, Df64>::value) {
+#pragma unroll
+    for (int m = 0; m < 5; m++) cc2[m] = df2(cc[m], cc[m]);
+  }
   // variable coefficients (operators 2-5): full precision, or BF16 with a
   // per-array scale in the mixed form (COMP selects BF16 for these operators)
   constexpr bool VAR = OpTraits<OP>::VAR;
@@ -451,6 +474,30 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
         for (int c = 0; c < CY; c++) {
           const T *srow = thr + ((RB * TT + (L - 1)) * PR + c * NTY) * PW;
           T val[VX];
+          // radius-1 constant-coefficient levels in FP32 or double-float: column
+          // pairs in packed f32x2 arithmetic (below)
+          constexpr bool PAIRS = std::is_same<T, float>::value && R == 1 && !VAR && (OP == 1 || OP == 8) &&
+                                 VX % 2 == 0;
+          constexpr bool DPAIRS = std::is_same<T, Df64>::value && R == 1 && !VAR && (OP == 1 || OP == 8) &&
+                                  VX % 2 == 0;
+          // their x neighbours across the group's edges are the last column of the
+          // lane to the left and the first column of the lane to the right, read by
+          // warp shuffles while the warp is still converged (at the region's x edges,
+          // and across a warp's row boundary, the value is one that the tile discards,
+          // as the unwritten shared-memory padding is)
+          [[maybe_unused]] T xe[2];
+          if constexpr (PAIRS || DPAIRS) {
+            constexpr unsigned kAll = 0xffffffffu;
+            if constexpr (PAIRS) {
+              xe[0] = __shfl_up_sync(kAll, q[L - 1][c][VX - 1][SL], 1);
+              xe[1] = __shfl_down_sync(kAll, q[L - 1][c][0][SL], 1);
+            } else {
+              xe[0] = T(__shfl_up_sync(kAll, q[L - 1][c][VX - 1][SL].hi, 1),
+                        __shfl_up_sync(kAll, q[L - 1][c][VX - 1][SL].lo, 1));
+              xe[1] = T(__shfl_down_sync(kAll, q[L - 1][c][0][SL].hi, 1),
+                        __shfl_down_sync(kAll, q[L - 1][c][0][SL].lo, 1));
+            }
+          }
           // rows outside level L's valid band (or halo planes) only carry their
           // value: a warp covers whole rows, so this branch is warp-uniform except
           // at the two x edges of the region
@@ -483,13 +530,11 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
             xrp.load(srow + VX);
           }
           // radius-1 constant-coefficient operators in FP32: column pairs in f32x2
-          constexpr bool PAIRS = std::is_same<T, float>::value && R == 1 && !VAR && (OP == 1 || OP == 8) &&
-                                 VX % 2 == 0;
           if constexpr (PAIRS) {
             static_for<VX / 2>([&](auto p_c) {
               constexpr int V0 = 2 * decltype(p_c)::value, V1 = V0 + 1;
-              const FusedAcc<R, T, QL, SL, VX, V0> a0{srow, q[L - 1][c], yv, xlp.e, xrp.e};
-              const FusedAcc<R, T, QL, SL, VX, V1> a1{srow, q[L - 1][c], yv, xlp.e, xrp.e};
+              const FusedAcc<R, T, QL, SL, VX, V0, true> a0{srow, q[L - 1][c], yv, xlp.e, xrp.e, xe};
+              const FusedAcc<R, T, QL, SL, VX, V1, true> a1{srow, q[L - 1][c], yv, xlp.e, xrp.e, xe};
               const float2 v2 = make_float2(a0.c(), a1.c());
               const float2 lap = star1_sum2(cc, v2, __fadd2_rn(make_float2(a0.x(1), a1.x(1)), make_float2(a0.x(-1), a1.x(-1))),
                                             __fadd2_rn(make_float2(a0.y(1), a1.y(1)), make_float2(a0.y(-1), a1.y(-1))),
@@ -509,6 +554,31 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
               const bool on1 = p_int && (act >> (((L - 1) * CY + c) * VX + V1) & 1u);
               val[V0] = on0 ? cand.x : v2.x;  // halo and out-of-region points keep their value
               val[V1] = on1 ? cand.y : v2.y;
+            });
+          } else if constexpr (DPAIRS) {
+            // double-float radius-1 constant-coefficient levels: column pairs with
+            // packed f32x2 arithmetic, each lane the scalar Df64 code's operations
+            static_for<VX / 2>([&](auto p_c) {
+              constexpr int V0 = 2 * decltype(p_c)::value, V1 = V0 + 1;
+              const FusedAcc<R, T, QL, SL, VX, V0, true> a0{srow, q[L - 1][c], yv, xlp.e, xrp.e, xe};
+              const FusedAcc<R, T, QL, SL, VX, V1, true> a1{srow, q[L - 1][c], yv, xlp.e, xrp.e, xe};
+              const PairAcc<FusedAcc<R, T, QL, SL, VX, V0, true>, FusedAcc<R, T, QL, SL, VX, V1, true>> acc2{a0, a1};
+              const Df2 centre = acc2.c();
+              const Df2 lap = star_grouped_sum<R, FastArith>(cc2, acc2);
+              Df2 cand;
+              if constexpr (TO == 2) {
+                Df2 uold;
+                if constexpr (L >= 2) uold = df2(q[L - 2][c][V0][SL], q[L - 2][c][V1][SL]);
+                else uold = df2(pvc[c].e[V0], pvc[c].e[V1]);
+                cand = (twice(centre) - uold) + df2(r2c[L - 1][c].e[V0], r2c[L - 1][c].e[V1]) * lap;
+              } else {
+                cand = lap;
+              }
+              cand = df_norm(cand);
+              const bool on0 = p_int && (act >> (((L - 1) * CY + c) * VX + V0) & 1u);
+              const bool on1 = p_int && (act >> (((L - 1) * CY + c) * VX + V1) & 1u);
+              val[V0] = on0 ? df2_x(cand) : df2_x(centre);  // halo and out-of-region points keep their value
+              val[V1] = on1 ? df2_y(cand) : df2_y(centre);
             });
           } else
           static_for<VX>([&](auto v_c) {

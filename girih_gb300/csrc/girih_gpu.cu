@@ -156,41 +156,63 @@ size_t host_array_elems(const girih_gpu_ctx *c) {
   return (size_t)c->d.ldomain_shape[0] * c->d.ldomain_shape[1] * c->d.ldomain_shape[2];
 }
 
-// Host (reference layout, element size hsz) -> device layout buffer (tsz).
-int upload_field(girih_gpu_ctx *c, const void *h, void *dst) {
+// Device address of a host array the GPU can reach directly (pinned or
+// registered host memory), else nullptr (pageable memory).
+const void *pinned_alias(const void *h) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+    cudaGetLastError();  // clear the sticky-free error of an unknown pointer
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// Layout kernel between host-layout src (element hsz) and device-layout dst (tsz).
+cudaError_t host_to_device_layout(const girih_gpu_ctx *c, const void *src, void *dst) {
   const Geom &g = c->g;
-  if (c->hsz == c->tsz) {
-    CK(cudaMemcpy2DAsync(static_cast<char *>(dst) + (size_t)g.ox * c->tsz, (size_t)g.px * c->tsz, h,
-                         (size_t)g.hpx * c->hsz, (size_t)g.nnx * c->tsz, (size_t)g.nny * g.nnz,
-                         cudaMemcpyHostToDevice, c->st));
+  if (c->hsz == 8 && c->tsz == 8) return launch_to_device_layout<double, double>(g, (const double *)src, (double *)dst, c->st);
+  if (c->hsz == 8) return launch_to_device_layout<double, float>(g, (const double *)src, (float *)dst, c->st);
+  if (c->tsz == 8) return launch_to_device_layout<float, double>(g, (const float *)src, (double *)dst, c->st);
+  return launch_to_device_layout<float, float>(g, (const float *)src, (float *)dst, c->st);
+}
+cudaError_t device_to_host_layout(const girih_gpu_ctx *c, const void *src, void *dst) {
+  const Geom &g = c->g;
+  if (c->hsz == 8 && c->tsz == 8) return launch_to_host_layout<double, double>(g, (const double *)src, (double *)dst, c->st);
+  if (c->hsz == 8) return launch_to_host_layout<float, double>(g, (const float *)src, (double *)dst, c->st);
+  if (c->tsz == 8) return launch_to_host_layout<double, float>(g, (const double *)src, (float *)dst, c->st);
+  return launch_to_host_layout<float, float>(g, (const float *)src, (float *)dst, c->st);
+}
+
+// Host (reference layout, element size hsz) -> device layout buffer (tsz).  A
+// pinned host array is read by the layout kernel itself (one pass over the
+// host link, no staging); a pageable one arrives by one contiguous copy into
+// the staging buffer, which the layout kernel then converts.
+int upload_field(girih_gpu_ctx *c, const void *h, void *dst) {
+  if (const void *dh = pinned_alias(h)) {
+    CK(host_to_device_layout(c, dh, dst));
     return 0;
   }
   size_t n = host_array_elems(c);
   int e = ensure_staging(c, n * 8);
   if (e) return e;
   CK(cudaMemcpyAsync(c->staging, h, n * c->hsz, cudaMemcpyHostToDevice, c->st));
-  if (c->hsz == 8)
-    CK(launch_to_device_layout<double, float>(g, (const double *)c->staging, (float *)dst, c->st));
-  else
-    CK(launch_to_device_layout<float, double>(g, (const float *)c->staging, (double *)dst, c->st));
+  CK(host_to_device_layout(c, c->staging, dst));
   return 0;
 }
 
+// Device layout -> host array.  Only the nnx columns of each row are written
+// (the caller's x padding is left as it is): directly by the layout kernel into
+// a pinned host array, else through the staging buffer and a row-wise copy.
 int download_field(girih_gpu_ctx *c, const void *src, void *h) {
   const Geom &g = c->g;
-  if (c->hsz == c->tsz) {
-    CK(cudaMemcpy2DAsync(h, (size_t)g.hpx * c->hsz, static_cast<const char *>(src) + (size_t)g.ox * c->tsz,
-                         (size_t)g.px * c->tsz, (size_t)g.nnx * c->tsz, (size_t)g.nny * g.nnz,
-                         cudaMemcpyDeviceToHost, c->st));
+  if (const void *dh = pinned_alias(h)) {
+    CK(device_to_host_layout(c, src, const_cast<void *>(dh)));
     return 0;
   }
   size_t n = host_array_elems(c);
   int e = ensure_staging(c, n * 8);
   if (e) return e;
-  if (c->hsz == 8)
-    CK(launch_to_host_layout<float, double>(g, (const float *)src, (double *)c->staging, c->st));
-  else
-    CK(launch_to_host_layout<double, float>(g, (const double *)src, (float *)c->staging, c->st));
+  CK(device_to_host_layout(c, src, c->staging));
   CK(cudaMemcpy2DAsync(h, (size_t)g.hpx * c->hsz, c->staging, (size_t)g.hpx * c->hsz,
                        (size_t)g.nnx * c->hsz, (size_t)g.nny * g.nnz, cudaMemcpyDeviceToHost, c->st));
   return 0;
@@ -721,7 +743,7 @@ int girih_gpu_download(girih_gpu_ctx *c, void *U1, void *U2) {
   DeviceGuard dg(c->d.device);
   int e;
   if (U1 && (e = download_field(c, c->f[c->iu1], U1))) return e;
-  if (U1 && U2 && c->hsz != c->tsz) CK(cudaStreamSynchronize(c->st));  // staging reuse
+  if (U1 && U2) CK(cudaStreamSynchronize(c->st));  // the staging buffer serves both arrays
   if (U2 && (e = download_field(c, c->f[c->iu2], U2))) return e;
   CK(cudaStreamSynchronize(c->st));
   return 0;
@@ -928,7 +950,7 @@ int girih_gpu_info(girih_gpu_ctx *c, girih_gpu_info_t *info) {
   info->bytes_per_lup = bytes;
   info->device_bytes = c->dev_bytes;
   std::snprintf(info->kernel_name, sizeof(info->kernel_name), "%s",
-                c->sched == GIRIH_SCHED_FUSED ? fused_kernel_name() : plain_kernel_name(g.op));
+                c->sched == GIRIH_SCHED_FUSED ? fused_kernel_name(g.op) : plain_kernel_name(g.op));
   return 0;
 }
 

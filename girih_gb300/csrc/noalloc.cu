@@ -132,8 +132,10 @@ extern "C" int girih_gpu_fused_run_noalloc(const girih_gpu_desc *d, void *U1, vo
                                            const double *coefs, int nt, void *stream) {
   if (!d || !U1 || !U2 || !coefs) return fail_na(GIRIH_GPU_EINVAL, "null argument");
   int r, to, nc, var;
-  if (op_info(d->target_kernel, &r, &to, &nc, &var) || var)
-    return fail_na(GIRIH_GPU_EUNSUPPORTED, "no fused kernel for operator " + std::to_string(d->target_kernel));
+  if (op_info(d->target_kernel, &r, &to, &nc, &var) || var ||
+      (d->target_kernel != 0 && d->target_kernel != 1 && d->target_kernel != 8))
+    return fail_na(GIRIH_GPU_EUNSUPPORTED,
+                   "the no-allocation entry point runs operators 0, 1 and 8, not " + std::to_string(d->target_kernel));
   const int nx = d->stencil_shape[0], ny = d->stencil_shape[1], nz = d->stencil_shape[2];
   if (nx < 1 || ny < 1 || nz < 1 || d->ldomain_shape[0] < nx + 2 * r || d->ldomain_shape[1] != ny + 2 * r ||
       d->ldomain_shape[2] != nz + 2 * r)

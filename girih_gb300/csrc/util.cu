@@ -38,26 +38,32 @@ int grid_for(int64_t n) {
   return (int)(b < 152 * 32 ? (b < 1 ? 1 : b) : 152 * 32);
 }
 
+// Layout conversion, one (k, j) row per CTA iteration: the row's nnx elements
+// are contiguous on both sides, so reads and writes coalesce (also when one
+// side is pinned host memory that the kernel reads or writes directly).
 template <class Tin, class Tout>
 __global__ void to_device_layout(Geom g, const Tin *__restrict__ src, Tout *__restrict__ dst) {
-  const int64_t n = (int64_t)g.nnx * g.nny * g.nnz;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    int i = (int)(t % g.nnx);
-    int64_t row = t / g.nnx;  // k*nny + j
-    dst[row * g.px + g.ox + i] = static_cast<Tout>(src[row * g.hpx + i]);
+  const int64_t rows = (int64_t)g.nny * g.nnz;
+  for (int64_t row = blockIdx.x; row < rows; row += gridDim.x) {
+    const Tin *s = src + row * g.hpx;
+    Tout *d = dst + row * g.px + g.ox;
+    for (int i = threadIdx.x; i < g.nnx; i += blockDim.x) d[i] = static_cast<Tout>(s[i]);
   }
 }
 
 template <class Tin, class Tout>
 __global__ void to_host_layout(Geom g, const Tin *__restrict__ src, Tout *__restrict__ dst) {
-  const int64_t n = (int64_t)g.nnx * g.nny * g.nnz;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    int i = (int)(t % g.nnx);
-    int64_t row = t / g.nnx;
-    dst[row * g.hpx + i] = static_cast<Tout>(src[row * g.px + g.ox + i]);
+  const int64_t rows = (int64_t)g.nny * g.nnz;
+  for (int64_t row = blockIdx.x; row < rows; row += gridDim.x) {
+    const Tin *s = src + row * g.px + g.ox;
+    Tout *d = dst + row * g.hpx;
+    for (int i = threadIdx.x; i < g.nnx; i += blockDim.x) d[i] = static_cast<Tout>(s[i]);
   }
+}
+
+int rows_grid(const Geom &g) {
+  const int64_t rows = (int64_t)g.nny * g.nnz;
+  return (int)(rows < 152 * 16 ? rows : 152 * 16);
 }
 
 __device__ __forceinline__ double nan_max(double a, double b) { return (a > b || a != a) ? a : b; }
@@ -195,12 +201,12 @@ __global__ void df_join_kernel(Geom g, const Df64 *__restrict__ in, double *__re
 
 template <class Tin, class Tout>
 cudaError_t launch_to_device_layout(const Geom &g, const Tin *src, Tout *dst, cudaStream_t s) {
-  to_device_layout<Tin, Tout><<<grid_for((int64_t)g.nnx * g.nny * g.nnz), kThreads, 0, s>>>(g, src, dst);
+  to_device_layout<Tin, Tout><<<rows_grid(g), kThreads, 0, s>>>(g, src, dst);
   return cudaGetLastError();
 }
 template <class Tin, class Tout>
 cudaError_t launch_to_host_layout(const Geom &g, const Tin *src, Tout *dst, cudaStream_t s) {
-  to_host_layout<Tin, Tout><<<grid_for((int64_t)g.nnx * g.nny * g.nnz), kThreads, 0, s>>>(g, src, dst);
+  to_host_layout<Tin, Tout><<<rows_grid(g), kThreads, 0, s>>>(g, src, dst);
   return cudaGetLastError();
 }
 template <class Tin>

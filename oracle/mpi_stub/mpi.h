@@ -5,9 +5,10 @@
  * GPU library includes it.
  *
  * Semantics are those of an MPI job with exactly one rank:
- *   - every Cartesian neighbour is MPI_PROC_NULL, so halo exchanges are no-ops
- *     (the reference only exchanges when a topology dimension is > 1,
- *     src/kernels/nb_naive_ts.c:32-155, src/kernels/diamond_ts.c:399-424);
+ *   - a Cartesian neighbour is the rank itself along a periodic dimension and
+ *     MPI_PROC_NULL otherwise; messages to itself are delivered (mpi_stub.c),
+ *     which the diamond stepper's periodic y exchanges need
+ *     (src/mpi_utils.c:66-80, src/kernels/diamond_ts.c:128-290);
  *   - reductions copy the send buffer (src/utils.c:844-860);
  *   - broadcasts and barriers do nothing;
  *   - MPI_Wtime is a monotonic wall clock (src/performance.c:74-78).
@@ -69,51 +70,26 @@ static inline double MPI_Wtime(void) {
   return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
 }
 
-static inline int MPI_Cart_create(MPI_Comm old, int nd, const int *dims, const int *periods,
-                                  int reorder, MPI_Comm *out) {
-  (void)old; (void)nd; (void)dims; (void)periods; (void)reorder; *out = MPI_COMM_WORLD; return 0;
-}
 static inline int MPI_Cart_coords(MPI_Comm c, int rank, int nd, int *coords) {
   (void)c; (void)rank; for (int i = 0; i < nd; i++) coords[i] = 0; return 0;
 }
-static inline int MPI_Cart_shift(MPI_Comm c, int dir, int disp, int *src, int *dst) {
-  (void)c; (void)dir; (void)disp; *src = MPI_PROC_NULL; *dst = MPI_PROC_NULL; return 0;
-}
 
-static inline int MPI_Type_create_subarray(int nd, const int *sizes, const int *subsizes,
-                                           const int *starts, int order, MPI_Datatype old,
-                                           MPI_Datatype *out) {
-  (void)nd; (void)sizes; (void)subsizes; (void)starts; (void)order; (void)old; *out = 0; return 0;
-}
-static inline int MPI_Type_contiguous(int n, MPI_Datatype old, MPI_Datatype *out) {
-  (void)n; (void)old; *out = 0; return 0;
-}
-static inline int MPI_Type_commit(MPI_Datatype *t) { (void)t; return 0; }
-static inline int MPI_Type_free(MPI_Datatype *t) { (void)t; return 0; }
-
-/* point-to-point: with one rank every peer is MPI_PROC_NULL, so nothing moves */
-static inline int MPI_Isend(const void *b, int n, MPI_Datatype t, int dst, int tag, MPI_Comm c,
-                            MPI_Request *r) {
-  (void)b; (void)n; (void)t; (void)dst; (void)tag; (void)c; *r = 0; return 0;
-}
-static inline int MPI_Irecv(void *b, int n, MPI_Datatype t, int src, int tag, MPI_Comm c,
-                            MPI_Request *r) {
-  (void)b; (void)n; (void)t; (void)src; (void)tag; (void)c; *r = 0; return 0;
-}
-static inline int MPI_Send(const void *b, int n, MPI_Datatype t, int dst, int tag, MPI_Comm c) {
-  (void)b; (void)n; (void)t; (void)dst; (void)tag; (void)c; return 0;
-}
-static inline int MPI_Recv(void *b, int n, MPI_Datatype t, int src, int tag, MPI_Comm c,
-                           MPI_Status *s) {
-  (void)b; (void)n; (void)t; (void)src; (void)tag; (void)c; (void)s; return 0;
-}
-static inline int MPI_Wait(MPI_Request *r, MPI_Status *s) { (void)r; (void)s; return 0; }
-static inline int MPI_Waitall(int n, MPI_Request *r, MPI_Status *s) {
-  (void)n; (void)r; (void)s; return 0;
-}
-static inline int MPI_Test(MPI_Request *r, int *flag, MPI_Status *s) {
-  (void)r; (void)s; *flag = 1; return 0;
-}
+/* Cartesian topology, datatypes and point-to-point messages: oracle/mpi_stub/mpi_stub.c
+ * (a rank's messages to itself along periodic dimensions; see there) */
+int MPI_Cart_create(MPI_Comm old, int nd, const int *dims, const int *periods, int reorder, MPI_Comm *out);
+int MPI_Cart_shift(MPI_Comm c, int dir, int disp, int *src, int *dst);
+int MPI_Type_create_subarray(int nd, const int *sizes, const int *subsizes, const int *starts, int order,
+                             MPI_Datatype old, MPI_Datatype *out);
+int MPI_Type_contiguous(int n, MPI_Datatype old, MPI_Datatype *out);
+int MPI_Type_commit(MPI_Datatype *t);
+int MPI_Type_free(MPI_Datatype *t);
+int MPI_Isend(const void *b, int n, MPI_Datatype t, int dst, int tag, MPI_Comm c, MPI_Request *r);
+int MPI_Irecv(void *b, int n, MPI_Datatype t, int src, int tag, MPI_Comm c, MPI_Request *r);
+int MPI_Send(const void *b, int n, MPI_Datatype t, int dst, int tag, MPI_Comm c);
+int MPI_Recv(void *b, int n, MPI_Datatype t, int src, int tag, MPI_Comm c, MPI_Status *s);
+int MPI_Wait(MPI_Request *r, MPI_Status *s);
+int MPI_Waitall(int n, MPI_Request *r, MPI_Status *s);
+int MPI_Test(MPI_Request *r, int *flag, MPI_Status *s);
 
 static inline int MPI_Reduce(const void *sb, void *rb, int n, MPI_Datatype t, MPI_Op op, int root,
                              MPI_Comm c) {

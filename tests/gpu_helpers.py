@@ -41,6 +41,26 @@ def gpu_context(g, **kw):
     return ctx
 
 
+def bf16_round(x):
+    """Round float64 values to the nearest BF16 number (8 significant bits, ties
+    to even), as __double2bfloat16 does for values in the normal range."""
+    m, e = np.frexp(np.asarray(x, dtype=np.float64))
+    return np.ldexp(np.rint(m * 256.0) / 256.0, e)
+
+
+def bf16_quantized_coefs(g):
+    """The coefficient arrays the mixed form computes with: per array a scale
+    s = FP32(max |c|), the BF16 value of c / s, and the effective coefficient
+    FP32(FP32(bf16) * s) (the kernels' load: bf16 -> float times the scale)."""
+    out = g.coef.copy()
+    for m in range(out.shape[0]):
+        c = g.coef[m]
+        s = np.float32(np.max(np.abs(c)))
+        q = bf16_round(c / np.float64(s)).astype(np.float32)
+        out[m] = (q * s).astype(np.float64)
+    return out
+
+
 def max_rel(a, b, g):
     n = oracle.norms(a, b, g)
     return n[0] / n[1] if n[1] > 0 else n[0]

@@ -73,12 +73,71 @@ def test_algorithmic_bytes(op, precision, schedule, want):
     assert bench.pass_bytes(gpu.OP_INFO[op], tsz, schedule, precision) == want
 
 
-def test_cpu_baseline_reports_its_sample():
+def test_port_baseline_reports_its_sample():
     wl = dict(bench.WORKLOADS["star7_leapfrog_512"], n=20)
-    cb = bench.cpu_baseline(wl, 0.05)
+    cb = bench.cpu_baseline_port(wl, 0.05)
     assert cb["kind"] == "port" and cb["unit"] == "GLUP/s" and cb["value"] > 0
-    assert cb["cores"] == (os.cpu_count() or 1)
+    assert cb["cores"] == bench.host_threads()
     assert cb["sample"].startswith("20^3 grid")
+
+
+needs_reference = pytest.mark.skipif(not bench.reference_binary_ok(), reason="reference build not present")
+
+
+@needs_reference
+def test_reference_binary_times_each_test():
+    """The reference's own MWD build, run as the CPU baseline: one time per
+    performance test, and MWD's raised nt read from its report."""
+    times, nt_eff, threads, cmd = bench.run_reference_binary(1, 32, 3, nt=10, threads=2)
+    assert len(times) == 3 and all(t > 0 for t in times)
+    assert nt_eff == 18  # 2 + a multiple of 2 (t_dim + 1) = 16 at t_dim 7
+    assert threads == 2 and "--target-ts 2" in cmd and "--mwd-type 2" in cmd
+
+
+@needs_reference
+@pytest.mark.parametrize("kernel", sorted(bench.REFERENCE_STEPPER))
+def test_reference_stepper_settings_pass_the_reference_verifier(kernel, tmp_path):
+    """The MWD settings timed as the CPU baseline compute what the reference's
+    serial operators compute (its own --verify 1, bit for bit on this x86-64
+    host, src/verification.c:842-849): a baseline that skipped work would fail."""
+    import subprocess
+    threads = min(4, os.cpu_count() or 1)
+    args = bench.fit_thread_groups(bench.REFERENCE_STEPPER[kernel]["args"], threads)
+    r = subprocess.run([bench.REFERENCE_BINARY, "--nx", "64", "--ny", "64", "--nz", "48", "--nt", "4",
+                        "--target-kernel", str(kernel), "--verify", "1"] + args, capture_output=True, text=True,
+                       env=dict(os.environ, OMP_NUM_THREADS=str(threads)), timeout=600, cwd=str(tmp_path))
+    assert r.returncode == 0 and "-PASSED" in r.stdout, r.stdout[-1500:] + r.stderr[-500:]
+
+
+def test_thread_groups_fit_the_host():
+    a = ["--target-ts", "2", "--thread-group-size", "8", "--thz", "8"]
+    assert bench.fit_thread_groups(a, 16) == a
+    assert bench.fit_thread_groups(a, 2)[3:] == ["2", "--thz", "2"]
+    assert bench.fit_thread_groups(a, 12)[3:] == ["6", "--thz", "6"]
+
+
+@needs_reference
+def test_cpu_baseline_is_the_reference_build(monkeypatch):
+    monkeypatch.setattr(bench, "host_threads", lambda: 2)
+    wl = dict(bench.WORKLOADS["star7_leapfrog_512"], n=32)
+    cb = bench.cpu_baseline(wl, 1.0, tests=2)
+    assert cb["kind"] == "reference" and cb["cores"] == 2 and cb["value"] > 0
+    assert "kernel 1" in cb["sample"] and "MWD" in cb["sample"] and "stands in" in cb["sample"]
+
+
+def test_reference_arm_shares_the_workload_config(monkeypatch):
+    """Both arms print the same config, so the two lines describe one workload;
+    the reference arm's steps are the samples it timed."""
+    monkeypatch.setattr(bench, "reference_binary_ok", lambda: False)
+    wl = dict(bench.WORKLOADS["star7_leapfrog_512"], n=16)
+
+    class A:
+        steps, warmup, cpu_seconds = 2, 1, 0.1
+    line = bench.run_reference(A, wl, 0, 1)
+    assert line["config"] == bench.workload_config(wl, 1)
+    assert line["impl"] == "reference" and line["steps"] == 2 and "sampled" in line
+    assert line["e2e"]["value"] == line["value"] and line["cpu_baseline"]["kind"] == "port"
+    assert bench.run_reference(A, wl, 1, 2) is None  # only rank 0 runs the CPU baseline
 
 
 def test_measured_peak_is_read_from_the_driver_file():

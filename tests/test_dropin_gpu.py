@@ -68,7 +68,7 @@ def _report(stdout):
 
 @pytest.mark.parametrize("kernel,precision,schedule", [(1, "fp64", "plain"), (1, "fp64df", "fused"),
                                                        (0, "mixed", "fused"), (5, "mixed", "plain"),
-                                                       (7, "fp64", "plain")])
+                                                       (7, "fp64", "plain"), (7, "fp64df", "fused")])
 def test_performance_run_reports_parse_py_keys(driver, tmp_path, kernel, precision, schedule):
     """The reference's performance harness timing the GPU stepper in each form
     (operator 8 has no reference id, so the reference CLI cannot name it)."""

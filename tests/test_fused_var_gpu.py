@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from girih_gb300 import gpu
-from gpu_helpers import fused_block, gpu_context, max_rel, oracle_grid
+from gpu_helpers import bf16_quantized_coefs, fused_block, gpu_context, max_rel, oracle_grid
 
 pytestmark = pytest.mark.gpu
 
@@ -68,17 +68,24 @@ def test_fused_var_mixed_matches_plain_mixed(op):
     g0 = oracle_grid(op, *_shape(op), seed=22)
     nt = 10
     ref = g0.copy().run(nt, nthreads=4)
+    # the FP64 oracle with the mixed form's own (BF16-quantised) coefficients
+    refq = g0.copy()
+    refq.coef[...] = bf16_quantized_coefs(g0)
+    refq.run(nt, nthreads=4)
     plain_u1, _ = _plain(g0, "mixed", nt)
     p32_u1, _ = _plain(g0, "fp32", nt)
     fp32_err = max_rel(p32_u1, ref.U1, ref)
     mixed_err = max_rel(plain_u1, ref.U1, ref)
+    assert max_rel(plain_u1, refq.U1, refq) < max(4 * fp32_err, 2e-6)
     for depth in range(1, _max_depth(op) + 1):
         with gpu_context(g0.copy(), precision="mixed", schedule="fused", fusion_depth=depth) as ctx:
             assert ctx.info()["bytes_per_lup"] == 8 + 2 * gpu.OP_INFO[op][2]
             ctx.run(nt)
             u1, _ = ctx.download()
-        # same BF16 coefficients: the two kernels differ by FP32 rounding only
+        # same BF16 coefficients: the two kernels differ by FP32 rounding only, and
+        # both sit within FP32 arithmetic error of the FP64 oracle with those coefficients
         assert max_rel(u1, plain_u1, ref) < max(4 * fp32_err, 2e-6), depth
+        assert max_rel(u1, refq.U1, refq) < max(4 * fp32_err, 2e-6), depth
         assert max_rel(u1, ref.U1, ref) < 2 * mixed_err + 1e-6, depth
 
 

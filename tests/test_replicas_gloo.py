@@ -40,11 +40,15 @@ def test_reference_arm_prints_once_under_torchrun():
     port = _free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.join(ROOT, "bench.py"),
-           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0", "--grid", "48", "--cpu-seconds", "0.3"]
+           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0", "--grid", "128", "--cpu-seconds", "0.3"]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
-    assert d["cpu_baseline"]["kind"] == "port"
+    # the reference's own build where it was compiled, else the oracle restatement
+    sys.path.insert(0, ROOT)
+    import bench
+    assert d["cpu_baseline"]["kind"] == ("reference" if bench.reference_binary_ok() else "port")
+    assert d["config"]["parallelism"] == "replicas2"

@@ -228,6 +228,7 @@ void fill_args(BatchGridArgs<T> &ga, const girih_gpu_ctx *c, int prev, int cur, 
   split_coefs(ga.a.cc, ga.a.cch, ga.a.ccl);
   ga.a.zchunk = zchunk;
   ga.a.write_prev = write_prev;
+  ga.a.range_flag = reinterpret_cast<unsigned *>(c->acc + 6);  // the grid's error word
   ga.op = c->g.op;
   ga.tt = tt;
 }
@@ -338,6 +339,8 @@ template <class T, bool COMP> int build_plan(girih_gpu_batch *b, int steps) {
 }
 
 int timed_graph(girih_gpu_batch *b, cudaGraphExec_t ex, float *ms_out) {
+  if (GIRIH_CHECKED)  // every grid's error word starts clear
+    for (auto *c : b->grids) B_CK(cudaMemsetAsync(c->acc + 6, 0, sizeof(unsigned), b->st));
   B_CK(cudaEventRecord(b->e0, b->st));
   if (ex) B_CK(cudaGraphLaunch(ex, b->st));
   B_CK(cudaEventRecord(b->e1, b->st));
@@ -346,6 +349,13 @@ int timed_graph(girih_gpu_batch *b, cudaGraphExec_t ex, float *ms_out) {
   float ms = 0;
   B_CK(cudaEventElapsedTime(&ms, b->e0, b->e1));
   if (ms_out) *ms_out = ms;
+  if (GIRIH_CHECKED) {
+    for (auto *c : b->grids) {
+      unsigned bad = 0;
+      B_CK(cudaMemcpy(&bad, c->acc + 6, sizeof(bad), cudaMemcpyDeviceToHost));
+      if (bad & kFlagBounds) return fail_b(GIRIH_GPU_EBOUNDS, "a kernel index left its array or shared block");
+    }
+  }
   return 0;
 }
 

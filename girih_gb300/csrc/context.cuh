@@ -45,6 +45,11 @@ struct girih_gpu_ctx {
   CUtensorMap tmaps[5][2];
   bool tmap_ok[5][2] = {{false, false}, {false, false}, {false, false}, {false, false}, {false, false}};
   int tmap_box[5][2][2] = {};  // box (x, y) each cached map was encoded with: a variant's box can change with depth
+  // checked build: per-buffer write counters (one per element) and the number
+  // of times the captured schedule writes each buffer's interior
+  unsigned *cov[4] = {nullptr, nullptr, nullptr, nullptr};
+  int run_expect[4] = {0, 0, 0, 0};  // of the steps last issued
+  int g_expect[4] = {0, 0, 0, 0};    // of the captured graph
 };
 
 namespace girih {

@@ -50,6 +50,7 @@ struct FusedLaunch {
   const double *src;       // source values per step (null: no source point)
   int src_off;             // device element offset of the source point
   int src_t0, src_n;       // step index of this pass's first level; number of values
+  unsigned *cov_prev, *cov_cur;  // checked build: write counters of out_prev / out_cur
 };
 
 bool fused_supported(const Geom &g, int precision);

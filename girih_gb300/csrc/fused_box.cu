@@ -50,6 +50,8 @@ __global__ void __launch_bounds__(NTX *NTY) fused_box_pass(FusedArgs<typename St
   extern __shared__ __align__(128) unsigned char smraw[];
   T *sm = reinterpret_cast<T *>(smraw);  // [2 buffers][TT levels][PR rows][PW columns]
   unsigned range_bad = 0;
+  unsigned *const flag = a.range_flag;                   // checked build: bounds violations
+  constexpr int64_t SMB = (int64_t)Sh::smem_bytes;
 
   const Geom &g = a.g;
   const int tx = threadIdx.x, ty = threadIdx.y;
@@ -127,8 +129,10 @@ __global__ void __launch_bounds__(NTX *NTY) fused_box_pass(FusedArgs<typename St
         for (int c = 0; c < CY; c++) {
           // F and E of level L-1 at plane p+1 (published at step s-1)
           const T *q = thr + ((RB * TT + (L - 1)) * PR + c * NTY) * PW;
-          f[L - 1][c][SP] = (q[-1] + q[1]) + (q[-PW] + q[PW]);
-          e[L - 1][c][SP] = (q[-PW - 1] + q[PW + 1]) + (q[-PW + 1] + q[PW - 1]);
+          if (in_shared(q - PW - 1, (int64_t)(2 * PW + 3) * sizeof(T), smraw, SMB, flag)) {
+            f[L - 1][c][SP] = (q[-1] + q[1]) + (q[-PW] + q[PW]);
+            e[L - 1][c][SP] = (q[-PW - 1] + q[PW + 1]) + (q[-PW + 1] + q[PW - 1]);
+          }
           const T centre = v[L - 1][c][S0];
           T val = centre;
           if (p_int && (act >> ((L - 1) * CY + c) & 1u)) {
@@ -145,8 +149,11 @@ __global__ void __launch_bounds__(NTX *NTY) fused_box_pass(FusedArgs<typename St
             else val = u;
           }
           if constexpr (L == TT || L == TT - 1) {
-            if (p_int && p >= Z0 && p < Z1 && x_out && y_out[c] && (L == TT || a.write_prev))
+            if (p_int && p >= Z0 && p < Z1 && x_out && y_out[c] && (L == TT || a.write_prev) &&
+                in_array(p * plane + col[c], 1, g.elems, flag)) {
               (L == TT ? a.out_cur : a.out_prev)[p * plane + col[c]] = to_storage<ST>(val);
+              count_writes(L == TT ? a.cov_cur : a.cov_prev, p * plane + col[c], 1);
+            }
           }
           if constexpr (L < TT) v[L][c][S0] = val;  // level L's newest plane is p
         }
@@ -156,18 +163,25 @@ __global__ void __launch_bounds__(NTX *NTY) fused_box_pass(FusedArgs<typename St
 #pragma unroll
       for (int c = 0; c < CY; c++) {
         T in = T(0);
-        if (s_in && x_dom && y_dom[c]) in = to_compute<T>(ldg_elem(a.cur + s * plane + col[c]), range_bad);
+        if (s_in && x_dom && y_dom[c] && in_array(s * plane + col[c], 1, g.elems, flag))
+          in = to_compute<T>(ldg_elem(a.cur + s * plane + col[c]), range_bad);
         v[0][c][qslot<QL>(PH)] = in;
         if constexpr (TT == 1) {
-          if (a.write_prev && s >= 1 && s < g.nnz - 1 && s >= Z0 && s < Z1 && x_out && y_out[c])
+          if (a.write_prev && s >= 1 && s < g.nnz - 1 && s >= Z0 && s < Z1 && x_out && y_out[c] &&
+              in_array(s * plane + col[c], 1, g.elems, flag)) {
             a.out_prev[s * plane + col[c]] = to_storage<ST>(in);
+            count_writes(a.cov_prev, s * plane + col[c], 1);
+          }
         }
       }
       // publish every level's newest plane (level l: plane s - 2l) for step s+1
 #pragma unroll
       for (int l = 0; l < TT; l++)
 #pragma unroll
-        for (int c = 0; c < CY; c++) thr[((WB * TT + l) * PR + c * NTY) * PW] = v[l][c][qslot<QL>(PH - 2 * l)];
+        for (int c = 0; c < CY; c++) {
+          T *const dst = thr + ((WB * TT + l) * PR + c * NTY) * PW;
+          if (in_shared(dst, sizeof(T), smraw, SMB, flag)) *dst = v[l][c][qslot<QL>(PH - 2 * l)];
+        }
       __syncthreads();
     });
   }
@@ -220,6 +234,8 @@ cudaError_t launch_box_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
   a.src_off = L.src_off;
   a.src_t0 = L.src_t0;
   a.src_n = L.src_n;
+  a.cov_prev = L.cov_prev;
+  a.cov_cur = L.cov_cur;
   a.zchunk = zchunk;
   a.write_prev = L.write_prev;
   fused_box_pass<T, TT, NTX, NTY, CY>

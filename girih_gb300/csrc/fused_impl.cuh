@@ -23,6 +23,7 @@
 #include <type_traits>
 #include <utility>
 
+#include "check.cuh"
 #include "df64.cuh"
 #include "fused.cuh"
 #include "ops.cuh"
@@ -47,6 +48,7 @@ template <class S> struct FusedArgs {
   const float *cscale;   // per-array scales of BF16 coefficients
   const double *src;     // source point values per step (null: none)
   int src_off, src_t0, src_n;
+  unsigned *cov_prev, *cov_cur;  // checked build: write counters of out_prev / out_cur (else null)
 };
 
 // Storage type of a compute type (every compute type is stored as itself).
@@ -277,6 +279,8 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
   constexpr int RW = Sh::RW, RY = Sh::RY, RP = Sh::RP, PW = Sh::PW, PR = Sh::PR, H = Sh::H, BX = Sh::BX,
                 BY = Sh::BY;
   unsigned range_bad = 0;
+  unsigned *const flag = a.range_flag;               // checked build: bounds violations
+  constexpr int64_t SMB = (int64_t)Sh::smem_bytes;   // shared allocation of the CTA
   static_assert(PW % VX == 0 && RP % VX == 0, "x groups must stay vector-aligned in shared memory");
   static_assert(BX > 0 && BY > 0, "tile too small for the fusion depth");
   static_assert(TT * CY * VX <= 32, "activity mask holds 32 (level, row, column) bits");
@@ -430,11 +434,15 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
           for (int c = 0; c < CY; c++) {
             const size_t off = (size_t)(ty + c * NTY) * RW + tx * VX;
             Pack<ST, VX> raw;
-            raw.load(ring_roc2 + (size_t)kr * RW * RY + off);
+#pragma unroll
+            for (int v = 0; v < VX; v++) raw.e[v] = ST(0);
+            const ST *pr = ring_roc2 + (size_t)kr * RW * RY + off;
+            if (in_shared(pr, VX * sizeof(ST), smraw, SMB, flag)) raw.load(pr);
 #pragma unroll
             for (int v = 0; v < VX; v++) r2c[l - 1][c].e[v] = to_compute<T>(raw.e[v], range_bad);
             if (l == 1) {
-              raw.load(ring_prev + (size_t)((s - s0) & (NB - 1)) * RW * RY + off);
+              const ST *pp = ring_prev + (size_t)((s - s0) & (NB - 1)) * RW * RY + off;
+              if (in_shared(pp, VX * sizeof(ST), smraw, SMB, flag)) raw.load(pp);
 #pragma unroll
               for (int v = 0; v < VX; v++) pvc[c].e[v] = to_compute<T>(raw.e[v], range_bad);
             }
@@ -453,7 +461,8 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
             if (l == 1)
 #pragma unroll
               for (int v = 0; v < VX; v++) pvc[c].e[v] = T(0);
-            if (p_int && ((act >> (((l - 1) * CY + c) * VX)) & ((1u << VX) - 1))) {
+            if (p_int && ((act >> (((l - 1) * CY + c) * VX)) & ((1u << VX) - 1)) &&
+                in_array(at, VX, g.elems, flag)) {
               r2c[l - 1][c].ldg(a.roc2 + at, range_bad);
               if (l == 1) pvc[c].ldg(a.prev + at, range_bad);
             }
@@ -501,7 +510,10 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
           // rows outside level L's valid band (or halo planes) only carry their
           // value: a warp covers whole rows, so this branch is warp-uniform except
           // at the two x edges of the region
-          const bool row_on = p_int && ((act >> (((L - 1) * CY + c) * VX)) & ((1u << VX) - 1));
+          const bool row_on = p_int && ((act >> (((L - 1) * CY + c) * VX)) & ((1u << VX) - 1)) &&
+                              in_shared(srow - R * PW - RP, (int64_t)(2 * R * PW + VX + 2 * RP) * sizeof(T), smraw,
+                                        SMB, flag) &&
+                              (!VAR || in_array(poff + col[c], VX, g.elems, flag));
           if (!row_on) {
 #pragma unroll
             for (int v = 0; v < VX; v++) val[v] = q[L - 1][c][v][SL];
@@ -643,17 +655,22 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
             }
           }
           if constexpr (L == TT || L == TT - 1) {
-            if (p_out && y_outr[c] && (L == TT || a.write_prev)) {
+            if (p_out && y_outr[c] && (L == TT || a.write_prev) && in_array(poff + col[c], VX, g.elems, flag)) {
               ST *dst = (L == TT ? a.out_cur : a.out_prev) + poff + col[c];
+              unsigned *cov = L == TT ? a.cov_cur : a.cov_prev;
               if (x_outc[0] && x_outc[VX - 1]) {
                 Pack<T, VX> o;
 #pragma unroll
                 for (int v = 0; v < VX; v++) o.e[v] = val[v];
                 o.stg(dst);
+                count_writes(cov, poff + col[c], VX);
               } else {
 #pragma unroll
                 for (int v = 0; v < VX; v++)
-                  if (x_outc[v]) dst[v] = to_storage<ST>(val[v]);
+                  if (x_outc[v]) {
+                    dst[v] = to_storage<ST>(val[v]);
+                    count_writes(cov, poff + col[c] + v, 1);
+                  }
               }
             }
           }
@@ -672,16 +689,20 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
         for (int v = 0; v < VX; v++) in.e[v] = T(0);
         if constexpr (TMA) {
           Pack<ST, VX> raw;  // out-of-range boxes are zero-filled by the copy
-          raw.load(ring_cur + (size_t)((s - s0) & (NB - 1)) * RW * RY + (size_t)(ty + c * NTY) * RW + tx * VX);
+#pragma unroll
+          for (int v = 0; v < VX; v++) raw.e[v] = ST(0);
+          const ST *pc = ring_cur + (size_t)((s - s0) & (NB - 1)) * RW * RY + (size_t)(ty + c * NTY) * RW + tx * VX;
+          if (in_shared(pc, VX * sizeof(ST), smraw, SMB, flag)) raw.load(pc);
 #pragma unroll
           for (int v = 0; v < VX; v++) in.e[v] = to_compute<T>(raw.e[v], range_bad);
         } else if (s_in && y_dom[c]) {
           if (xg_dom) {
-            in.ldg(a.cur + soff + col[c], range_bad);
+            if (in_array(soff + col[c], VX, g.elems, flag)) in.ldg(a.cur + soff + col[c], range_bad);
           } else {
 #pragma unroll
             for (int v = 0; v < VX; v++)
-              if (x_dom[v]) in.e[v] = to_compute<T>(ldg_elem(a.cur + soff + col[c] + v), range_bad);
+              if (x_dom[v] && in_array(soff + col[c] + v, 1, g.elems, flag))
+                in.e[v] = to_compute<T>(ldg_elem(a.cur + soff + col[c] + v), range_bad);
           }
         }
 #pragma unroll
@@ -690,7 +711,10 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
           if (a.write_prev && s >= R && s < g.nnz - R && s >= Z0 && s < Z1 && y_outr[c])
 #pragma unroll
             for (int v = 0; v < VX; v++)
-              if (x_outc[v]) a.out_prev[soff + col[c] + v] = to_storage<ST>(in.e[v]);
+              if (x_outc[v] && in_array(soff + col[c] + v, 1, g.elems, flag)) {
+                a.out_prev[soff + col[c] + v] = to_storage<ST>(in.e[v]);
+                count_writes(a.cov_prev, soff + col[c] + v, 1);
+              }
         }
       }
       // publish each level's centre plane (s - l*D - R) for the x/y neighbours of step s+1
@@ -701,7 +725,8 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
           Pack<T, VX> o;
 #pragma unroll
           for (int v = 0; v < VX; v++) o.e[v] = q[l][c][v][qslot<QL>(PH - l * D - R)];
-          o.store(thr + ((WB * TT + l) * PR + c * NTY) * PW);
+          T *const dst = thr + ((WB * TT + l) * PR + c * NTY) * PW;
+          if (in_shared(dst, VX * sizeof(T), smraw, SMB, flag)) o.store(dst);
         }
       __syncthreads();
     });
@@ -788,6 +813,8 @@ cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
   a.src_off = L.src_off;
   a.src_t0 = L.src_t0;
   a.src_n = L.src_n;
+  a.cov_prev = L.cov_prev;
+  a.cov_cur = L.cov_cur;
   a.zchunk = zchunk;
   a.write_prev = L.write_prev;
   if constexpr (TMA) {

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "internal.cuh"
+#include "check.cuh"
 #include "fused.cuh"
 
 namespace girih {
@@ -344,23 +345,32 @@ template <class T> StepArgs<T> step_args(girih_gpu_ctx *c, void *u, const void *
 int issue_steps_impl(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *iu2, cudaStream_t st) {
   *launches = 0;
   const bool exact = c->d.exact != 0;
+  unsigned *flag = reinterpret_cast<unsigned *>(c->acc + 6);
+  // the checked build's write counters: how often these steps write each buffer
+  for (int b = 0; b < 4; b++) c->run_expect[b] = 0;
   if (c->sched == GIRIH_SCHED_PLAIN) {
     for (int s = 0; s < steps; s += 2) {
       for (int h = 0; h < 2; h++) {
-        void *u = c->f[h == 0 ? *iu1 : *iu2];
+        const int ub = h == 0 ? *iu1 : *iu2;
+        void *u = c->f[ub];
         const void *v = c->f[h == 0 ? *iu2 : *iu1];
         const int sweep = s + h;
         const double *src = c->d_src && sweep < c->src_n ? c->d_src + sweep : nullptr;
+        c->run_expect[ub]++;
         cudaError_t e;
         if (c->tsz == 8) {
           StepArgs<double> a = step_args<double>(c, u, v);
           a.src = src;
           a.src_off = c->src_off;
+          a.flag = flag;
+          a.cov = c->cov[ub];
           e = launch_plain<double>(a, exact, false, st);
         } else {
           StepArgs<float> a = step_args<float>(c, u, v);
           a.src = src;
           a.src_off = c->src_off;
+          a.flag = flag;
+          a.cov = c->cov[ub];
           e = launch_plain<float>(a, exact, c->bf16coef, st);
         }
         if (e != cudaSuccess) return fail(GIRIH_GPU_ECUDA, std::string("plain launch: ") + cudaGetErrorString(e));
@@ -373,7 +383,6 @@ int issue_steps_impl(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *
   // newest states into the two spare buffers
   const bool dfp = c->d.precision == GIRIH_FP64_DF;
   void *const *buf = dfp ? c->dfp : c->f;
-  unsigned *flag = reinterpret_cast<unsigned *>(c->acc + 6);
   if (dfp && steps > 0) {
     // FP64 -> pairs: both states, the spares (whose halos the passes read), roc2
     int sp[2], n = 0;
@@ -405,6 +414,10 @@ int issue_steps_impl(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *
     // time order 1 never reads state t-1, so only the last pass writes it (U1)
     L.write_prev = (c->g.to == 2 || left == T) ? 1 : 0;
     L.range_flag = flag;
+    L.cov_prev = c->cov[spare[0]];
+    L.cov_cur = c->cov[spare[1]];
+    c->run_expect[spare[1]]++;
+    if (L.write_prev) c->run_expect[spare[0]]++;
     L.coef = c->coef;
     L.cscale = c->scale;
     if (c->d_src && c->src_n > 0) {
@@ -467,6 +480,8 @@ const char *girih_gpu_strerror(int err) {
     case GIRIH_GPU_ETIMEOUT: return "device-side wait timed out";
     case GIRIH_GPU_ENODEV: return "no usable CUDA device";
     case GIRIH_GPU_ERANGE: return "value outside the range of the selected precision";
+    case GIRIH_GPU_EBOUNDS: return "bounds-checked build: a kernel index left its array or shared block";
+    case GIRIH_GPU_ECOVERAGE: return "bounds-checked build: a point was not written exactly once per step";
   }
   return "unknown error";
 }
@@ -555,6 +570,9 @@ int girih_gpu_create(girih_gpu_ctx **out, const girih_gpu_desc *d) {
     if (c->bf16coef && (e = dev_alloc(c, (void **)&c->scale, 64 * sizeof(float)))) return bail(e);
   }
   if ((e = dev_alloc(c, (void **)&c->acc, 64))) return bail(e);
+  if (GIRIH_CHECKED)  // write counters of the four state buffers
+    for (int b = 0; b < 4; b++)
+      if ((e = dev_alloc(c, (void **)&c->cov[b], (size_t)c->g.elems * sizeof(unsigned)))) return bail(e);
   if (sched == GIRIH_SCHED_FUSED && (e = ensure_fused_buffers(c))) return bail(e);
   if (cudaStreamSynchronize(c->st) != cudaSuccess) return bail(fail(GIRIH_GPU_ECUDA, "initial clear failed"));
   *out = c;
@@ -577,6 +595,8 @@ void girih_gpu_destroy(girih_gpu_ctx *c) {
   if (c->scale) cudaFree(c->scale);
   if (c->staging) cudaFree(c->staging);
   if (c->acc) cudaFree(c->acc);
+  for (unsigned *p : c->cov)
+    if (p) cudaFree(p);
   if (c->e0) cudaEventDestroy(c->e0);
   if (c->e1) cudaEventDestroy(c->e1);
   if (c->st) cudaStreamDestroy(c->st);
@@ -706,11 +726,17 @@ int girih_gpu_run(girih_gpu_ctx *c, int nt, float *ms_out) {
     c->g_launches = launches;
     c->g_new_iu1 = a;
     c->g_new_iu2 = b;
+    for (int k = 0; k < 4; k++) c->g_expect[k] = c->run_expect[k];
   }
-  const bool df = c->sched == GIRIH_SCHED_FUSED &&
-                  (c->d.precision == GIRIH_FP64_DF || c->fcfg.box_w > 0);  // kernels that report through the flag
+  // kernels that report through the flag word: the double-float split, the TMA
+  // waits, and every kernel of the checked build
+  const bool df = GIRIH_CHECKED ||
+                  (c->sched == GIRIH_SCHED_FUSED && (c->d.precision == GIRIH_FP64_DF || c->fcfg.box_w > 0));
   unsigned *range_flag = reinterpret_cast<unsigned *>(c->acc + 6);
   if (df) CK(cudaMemsetAsync(range_flag, 0, sizeof(unsigned), c->st));
+  if (GIRIH_CHECKED)  // write counters start from zero (autotuner trials and looped batch runs also count)
+    for (int k = 0; k < 4; k++)
+      if (c->cov[k]) CK(cudaMemsetAsync(c->cov[k], 0, (size_t)c->g.elems * sizeof(unsigned), c->st));
   CK(cudaEventRecord(c->e0, c->st));
   if (steps > 0) CK(cudaGraphLaunch(c->gexec, c->st));
   CK(cudaEventRecord(c->e1, c->st));
@@ -719,12 +745,19 @@ int girih_gpu_run(girih_gpu_ctx *c, int nt, float *ms_out) {
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, c->e0, c->e1));
   if (ms_out) *ms_out = ms;
+  if (GIRIH_CHECKED && steps > 0)
+    for (int k = 0; k < 4; k++)
+      if (c->cov[k]) CK(launch_coverage_check(c->g, c->cov[k], (unsigned)c->g_expect[k], range_flag, c->st));
   if (df) {
     unsigned bad = 0;
-    CK(cudaMemcpy(&bad, range_flag, sizeof(bad), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(&bad, range_flag, sizeof(bad), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
     if (bad) {
       c->iu1 = c->g_new_iu1;
       c->iu2 = c->g_new_iu2;
+      if (bad & kFlagBounds) return fail(GIRIH_GPU_EBOUNDS, "a kernel index left its array or shared block");
+      if (bad & kFlagCoverage)
+        return fail(GIRIH_GPU_ECOVERAGE, "a point was not written exactly as often as the schedule writes it");
       if (bad & 2u) return fail(GIRIH_GPU_ETIMEOUT, "a TMA plane copy did not complete within the wait bound");
       return fail(GIRIH_GPU_ERANGE, "a field value left the FP32 exponent range of the double-float fused kernel; "
                                     "use GIRIH_FP64 for this grid");

@@ -42,6 +42,8 @@ template <class T> struct StepArgs {
   T cc[5];            // constant coefficients
   const double *src;  // source point: value of this sweep at src[0] (null: no update)
   int64_t src_off;    // device element offset of the source point
+  unsigned *flag;     // checked build: error word (bounds violations)
+  unsigned *cov;      // checked build: write counters of u
 };
 
 // Plain (one step per launch) kernels: plain.cu
@@ -76,6 +78,10 @@ cudaError_t launch_df_split(const Geom &g, const double *in, void *out0, void *o
 cudaError_t launch_df_join(const Geom &g, const void *in, double *out, cudaStream_t s);
 cudaError_t launch_halo_equal(const Geom &g, const void *a, const void *b, int tsz,
                               unsigned int *flag, cudaStream_t s);
+// Checked build: every interior point of a buffer must have been written
+// `expect` times and no other point at all (else kFlagCoverage in *flag); the
+// counters are cleared for the next run.
+cudaError_t launch_coverage_check(const Geom &g, unsigned *cov, unsigned expect, unsigned *flag, cudaStream_t s);
 
 // Per-thread error detail.
 void set_error(const std::string &msg);

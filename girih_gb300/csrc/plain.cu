@@ -13,6 +13,7 @@
 // roughly a quarter of the load instructions of the one-column sweep.
 #include <algorithm>
 
+#include "check.cuh"
 #include "internal.cuh"
 #include "ops.cuh"
 #include "vec.cuh"
@@ -51,9 +52,15 @@ __global__ void __launch_bounds__(kBX *kBY) plain_step(StepArgs<T> a, Cf coef, i
 #pragma unroll
   for (int m = 0; m < 5; m++) cc[m] = a.cc[m];
   T q[2 * R + 1];
+  // checked build: the point's whole neighbourhood block, planes k-R..k+R
+  const int64_t reach = R * plane + R * (int64_t)a.g.px + R;
 #pragma unroll
-  for (int d = 0; d < 2 * R; d++) q[d] = __ldg(a.v + c + (int64_t)(d - R) * plane);
+  for (int d = 0; d < 2 * R; d++) q[d] = T(0);
+  if (in_array(c - reach, 2 * reach + 1, a.g.elems, a.flag))
+#pragma unroll
+    for (int d = 0; d < 2 * R; d++) q[d] = __ldg(a.v + c + (int64_t)(d - R) * plane);
   for (int k = k0; k < k1; k++, c += plane) {
+    if (!in_array(c - reach, 2 * reach + 1, a.g.elems, a.flag)) continue;
     q[2 * R] = __ldg(a.v + c + (int64_t)R * plane);
     ColumnAcc<R, T> acc{a.v + c, a.g.px, plane, q};
     T uold = T(0), r2 = T(0);
@@ -62,6 +69,7 @@ __global__ void __launch_bounds__(kBX *kBY) plain_step(StepArgs<T> a, Cf coef, i
       r2 = __ldg(a.roc2 + c);
     }
     a.u[c] = apply_op<OP, A>(cc, coef, c, acc, uold, r2);
+    count_writes(a.cov, c, 1);
 #pragma unroll
     for (int d = 0; d < 2 * R; d++) q[d] = q[d + 1];
   }
@@ -109,19 +117,31 @@ __global__ void __launch_bounds__(kBX *kBY) plain_step_quad(StepArgs<T> a, int z
 #pragma unroll
   for (int m = 0; m < 5; m++) cc[m] = a.cc[m];
   T q[2 * R + 1][VX];
+  unsigned *const flag = a.flag;
+  const int64_t n = a.g.elems;
+  // checked build: each vector access range inside the array (a load outside is skipped)
+  auto ld = [&](int64_t off, T(&e)[VX]) {
+    if (in_array(off, VX, n, flag)) {
+      vload<T, VX>(a.v + off, e);
+    } else {
 #pragma unroll
-  for (int d = 0; d < 2 * R; d++) vload<T, VX>(a.v + c + (int64_t)(d - R) * plane, q[d]);
+      for (int v = 0; v < VX; v++) e[v] = T(0);
+    }
+  };
+#pragma unroll
+  for (int d = 0; d < 2 * R; d++) ld(c + (int64_t)(d - R) * plane, q[d]);
   const bool full = i0 + VX <= a.g.nx;
   for (int k = k0; k < k1; k++, c += plane) {
-    vload<T, VX>(a.v + c + (int64_t)R * plane, q[2 * R]);
+    ld(c + (int64_t)R * plane, q[2 * R]);
     T xl[VX], xr[VX], yv[2 * R][VX];
-    vload<T, VX>(a.v + c - VX, xl);
-    vload<T, VX>(a.v + c + VX, xr);
+    ld(c - VX, xl);
+    ld(c + VX, xr);
 #pragma unroll
     for (int d = 1; d <= R; d++) {
-      vload<T, VX>(a.v + c + d * px, yv[d - 1]);
-      vload<T, VX>(a.v + c - d * px, yv[R + d - 1]);
+      ld(c + d * px, yv[d - 1]);
+      ld(c - d * px, yv[R + d - 1]);
     }
+    if (!in_array(c, VX, n, flag)) continue;  // the old value, roc2, coefficients and the store
     T uo[VX], r2[VX];
     if constexpr (TO == 2) {
       VecU<T, VX> u;
@@ -153,10 +173,14 @@ __global__ void __launch_bounds__(kBX *kBY) plain_step_quad(StepArgs<T> a, int z
 #pragma unroll
       for (int v = 0; v < VX; v++) u.e[v] = out[v];
       *reinterpret_cast<decltype(u.v) *>(a.u + c) = u.v;
+      count_writes(a.cov, c, VX);
     } else {
 #pragma unroll
       for (int v = 0; v < VX; v++)
-        if (i0 + v < a.g.nx) a.u[c + v] = out[v];
+        if (i0 + v < a.g.nx) {
+          a.u[c + v] = out[v];
+          count_writes(a.cov, c + v, 1);
+        }
     }
 #pragma unroll
     for (int d = 0; d < 2 * R; d++)

@@ -1,6 +1,7 @@
 // Data movement and reduction kernels: layout conversion between the
 // reference's host layout and the device layout, BF16 quantisation, seeded
 // initialisation and the FP64 error norms used by verification.
+#include "check.cuh"
 #include "df64.cuh"
 #include "internal.cuh"
 
@@ -197,7 +198,26 @@ __global__ void df_join_kernel(Geom g, const Df64 *__restrict__ in, double *__re
     out[at] = df_to_double(Df64(v.x, v.y));
   }
 }
+// Checked build: every interior point written `expect` times, nothing else
+// written at all; the counters are cleared.
+__global__ void coverage_check_kernel(Geom g, unsigned *cov, unsigned expect, unsigned *flag) {
+  const int64_t n = g.elems;
+  unsigned bad = 0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = t / g.plane, rem = t - k * g.plane;
+    const int64_t j = rem / g.px, i = rem - j * g.px - g.ox;  // i: index along x with the halo at 0..r-1
+    const bool interior = i >= g.r && i < g.nnx - g.r && j >= g.r && j < g.nny - g.r && k >= g.r && k < g.nnz - g.r;
+    if (cov[t] != (interior ? expect : 0u)) bad = 1;
+    cov[t] = 0;
+  }
+  if (bad) atomicOr(flag, kFlagCoverage);
+}
 }  // namespace
+
+cudaError_t launch_coverage_check(const Geom &g, unsigned *cov, unsigned expect, unsigned *flag, cudaStream_t s) {
+  coverage_check_kernel<<<grid_for(g.elems), kThreads, 0, s>>>(g, cov, expect, flag);
+  return cudaGetLastError();
+}
 
 template <class Tin, class Tout>
 cudaError_t launch_to_device_layout(const Geom &g, const Tin *src, Tout *dst, cudaStream_t s) {

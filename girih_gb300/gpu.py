@@ -15,7 +15,10 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libgirih_gpu.so")
+# GIRIH_GPU_CHECKED=1 selects the bounds-checked build (build.py --checked):
+# every kernel access range tested against its buffer, write-coverage counters
+CHECKED = os.environ.get("GIRIH_GPU_CHECKED", "0") not in ("", "0")
+LIB_PATH = os.path.join(HERE, "libgirih_gpu_check.so" if CHECKED else "libgirih_gpu.so")
 
 FP64, FP32, MIXED, FP64_DF = 0, 1, 2, 3
 PLAIN, FUSED, AUTO = 0, 1, 2
@@ -27,7 +30,7 @@ OP_INFO = {0: (4, 2, 5, False), 1: (1, 1, 2, False), 2: (1, 1, 2, True), 3: (1, 
            4: (4, 1, 13, True), 5: (1, 1, 7, True), 7: (1, 1, 4, False), 8: (1, 2, 2, False)}
 
 ERRORS = {1: "EINVAL", 2: "EUNSUPPORTED", 3: "ECUDA", 4: "ENOMEM", 5: "ESTATE", 6: "ETIMEOUT", 7: "ENODEV",
-          8: "ERANGE"}
+          8: "ERANGE", 9: "EBOUNDS", 10: "ECOVERAGE"}
 
 
 class Desc(ctypes.Structure):
@@ -59,7 +62,8 @@ def lib():
     global _lib
     if _lib is None:
         if not os.path.exists(LIB_PATH):
-            raise ImportError(f"{LIB_PATH} is missing: build it with `python girih_gb300/build.py`")
+            how = "python girih_gb300/build.py" + (" --checked" if CHECKED else "")
+            raise ImportError(f"{LIB_PATH} is missing: build it with `{how}`")
         L = ctypes.CDLL(LIB_PATH)
         P = ctypes.c_void_p
         L.girih_gpu_create.argtypes = [ctypes.POINTER(P), ctypes.POINTER(Desc)]

@@ -50,7 +50,11 @@ enum {
   GIRIH_GPU_ESTATE = 5,       /* call out of order (e.g. run before upload) */
   GIRIH_GPU_ETIMEOUT = 6,     /* a bounded device-side wait gave up */
   GIRIH_GPU_ENODEV = 7,       /* no usable CUDA device */
-  GIRIH_GPU_ERANGE = 8        /* a value left the range the selected precision can carry */
+  GIRIH_GPU_ERANGE = 8,       /* a value left the range the selected precision can carry */
+  GIRIH_GPU_EBOUNDS = 9,      /* bounds-checked build (libgirih_gpu_check.so): a kernel index left
+                                 its array or shared-memory block; the access was skipped */
+  GIRIH_GPU_ECOVERAGE = 10    /* bounds-checked build: a point was written other than once per step
+                                 (or a halo / padding point was written) */
 };
 
 enum { GIRIH_OP_STAR7_LEAPFROG = 8 };

@@ -1,6 +1,6 @@
 /*
  * Single-rank stand-in for <mpi.h>, used only to compile the unmodified girih
- * reference sources (src/driver.c, src/utils.c, src/kernels/*.c, ...) into the
+ * reference sources (src/driver.c, src/utils.c, the src/kernels sources, ...) into the
  * CPU oracle and CPU baseline binary.  It is test infrastructure: nothing in the
  * GPU library includes it.
  *

@@ -41,10 +41,11 @@ struct girih_gpu_ctx {
   int g_launches = 0, g_new_iu1 = 0, g_new_iu2 = 1;
   int last_launches = 0, last_steps = 0;
   double dev_bytes = 0;
-  // TMA tensor maps of the four field buffers and roc2 (index 4), per TMA variant (2, 3)
+  // TMA tensor maps of the four field buffers and roc2 (index 4), per TMA variant (2, 3; double-float 5, 6)
   CUtensorMap tmaps[5][2];
   bool tmap_ok[5][2] = {{false, false}, {false, false}, {false, false}, {false, false}, {false, false}};
   int tmap_box[5][2][2] = {};  // box (x, y) each cached map was encoded with: a variant's box can change with depth
+  const void *tmap_base[5][2] = {};  // array each cached map was encoded for
   // checked build: per-buffer write counters (one per element) and the number
   // of times the captured schedule writes each buffer's interior
   unsigned *cov[4] = {nullptr, nullptr, nullptr, nullptr};

@@ -72,12 +72,31 @@ static FusedConfig make_box_config(int precision, int depth, int variant) {
   return c;
 }
 
+// Double-float radius-1 constant-coefficient operators (1, 8), variants 5 and 6:
+// the TMA-staged kernel of fused_df_tma.cu (32 rows, 32 or 64 columns, depth
+// <= 2).  Its boxes start on 16 bytes (2 columns), so the tile is the aligned
+// width where that loses nothing (depth 2) and the general one else.
+static FusedConfig make_df_tma_config(const Geom &g, int depth, int variant) {
+  FusedConfig c{};
+  if (g.r != 1 || g.var || g.op == 7 || depth > 2) return c;
+  const int cols = df_tma_cols(variant), rows = df_tma_rows(variant);
+  if (df_tma_smem(g.to, depth, cols, rows) > (size_t)227 * 1024) return c;
+  c.depth = depth;
+  c.variant = variant;
+  c.bx = fused_tile_width(cols, depth, 2, false);
+  c.by = rows - 2 * depth;
+  c.box_w = cols;
+  c.box_h = rows;
+  return c;
+}
+
 FusedConfig make_fused_config(const Geom &g, int precision, int depth, int variant) {
   FusedConfig c{};
   if (!fused_supported(g, precision) || depth < 1 || depth > fused_max_depth(g, precision) ||
       variant < 0 || variant >= FV_COUNT)
     return c;
   if (g.op == 7) return make_box_config(precision, depth, variant);
+  if (variant >= 5) return precision == GIRIH_FP64_DF ? make_df_tma_config(g, depth, variant) : c;
   int ntx, ry, vx;
   variant_shape(variant, g.r, precision, &ntx, &ry, &vx);
   if (variant == 2 && precision != GIRIH_FP64_DF && ((g.r == 1 && depth == 4) || (g.r == 4 && depth == 1)))
@@ -117,7 +136,11 @@ FusedConfig choose_fused_config(const Geom &g, int precision, int depth, int bx,
   int d = depth;
   if (d <= 0) d = g.r == 4 ? 2 : (precision == GIRIH_FP64 ? 2 : 4);
   d = d > fused_max_depth(g, precision) ? fused_max_depth(g, precision) : d;
-  for (int v = 0; v < FV_COUNT; v++) {
+  // double-float: the TMA-staged variants first, so that a tile they share with
+  // a register variant (28 x 28 and 60 x 28 at depth 2) selects them
+  static const int df_order[FV_COUNT] = {5, 6, 0, 1, 2, 3, 4};
+  for (int k = 0; k < FV_COUNT; k++) {
+    const int v = precision == GIRIH_FP64_DF ? df_order[k] : k;
     FusedConfig c = make_fused_config(g, precision, d, v);
     if (!c.depth) continue;
     if ((bx && bx != c.bx) || (by && by != c.by)) continue;
@@ -160,6 +183,10 @@ cudaError_t launch_fused(const Geom &g, int tsz, int precision, const FusedConfi
   return cudaErrorInvalidValue;
 }
 
-const char *fused_kernel_name(int op) { return op == 7 ? "fused_box_pass" : "fused_pass"; }
+const char *fused_kernel_name(int op, int precision, const FusedConfig &cfg) {
+  if (op == 7) return "fused_box_pass";
+  if (precision == GIRIH_FP64_DF && cfg.variant >= 5) return "fused_df_tma";
+  return cfg.box_w > 0 ? "fused_pass_tma" : "fused_pass";
+}
 
 }  // namespace girih

@@ -10,9 +10,9 @@ namespace girih {
 // variants 0 and 1 with the input planes staged into shared memory by TMA
 // (FP32 storage; variant 2 switches to x quads at radius-1 depth 4 and
 // radius-4 depth 1, variant 3 to a 64 x 64 region with x quads at radius-1
-// depth <= 2).  The double-float form numbers its own five shapes 0-4, see
-// variant_shape in fused.cu.
-enum FusedVariant { FV_64x32_512 = 0, FV_32x64_1024 = 1, FV_64x32_512_TMA = 2, FV_32x64_1024_TMA = 3, FV_COUNT = 5 };
+// depth <= 2).  The double-float form numbers its own shapes: 0-4 (see
+// variant_shape in fused.cu) and the TMA-staged 5 and 6 below.
+enum FusedVariant { FV_64x32_512 = 0, FV_32x64_1024 = 1, FV_64x32_512_TMA = 2, FV_32x64_1024_TMA = 3, FV_COUNT = 7 };
 
 // TMA ring depths: NB planes of the input (and old) state in flight (two for
 // deep passes and large regions, whose rings would not fit shared memory
@@ -25,6 +25,23 @@ __host__ __device__ constexpr int fused_tma_nr(int r, int tt, int nb) {
   int need = (tt - 1) * (r + 1) + nb, p = 1;
   while (p < need) p *= 2;
   return p;
+}
+
+// Double-float TMA passes (radius 1, constant coefficients; fused_df_tma.cu):
+// one column and two adjacent rows per thread, region df_tma_cols x 32 rows
+// (variant 5: 32 columns, variant 6: 64), depth <= 2.  Their rings: the input
+// state holds planes s-2 .. s+1 (level 1 reads its x/y neighbours there), in
+// 4 slots when the z queues are 4 planes long (time order 2) and 6 when they
+// are 3 (so that one unrolled z period, lcm(queue, ring, 2), stays short); the
+// old state 2 slots; roc2 2*depth slots (level l reads roc2 of plane s - l*D,
+// loaded with the input plane s - (l-1)*D).
+__host__ __device__ constexpr int df_tma_cols(int variant) { return variant == 5 ? 32 : 64; }
+__host__ __device__ constexpr int df_tma_rows(int) { return 32; }
+__host__ __device__ constexpr int df_tma_nb(int to) { return to == 2 ? 4 : 6; }
+__host__ __device__ constexpr int df_tma_nr(int tt) { return 2 * tt; }
+__host__ __device__ constexpr size_t df_tma_smem(int to, int tt, int cols, int rows) {
+  return ((size_t)2 * (tt - 1) * cols * rows * 8 + 127) / 128 * 128 +
+         (size_t)(df_tma_nb(to) + (to == 2 ? 2 + df_tma_nr(tt) : 0)) * cols * rows * 8 + (size_t)df_tma_nb(to) * 8;
 }
 
 struct FusedConfig {
@@ -59,7 +76,11 @@ FusedConfig make_fused_config(const Geom &g, int precision, int depth, int varia
 FusedConfig choose_fused_config(const Geom &g, int precision, int depth, int bx, int by);
 cudaError_t launch_fused(const Geom &g, int tsz, int precision, const FusedConfig &cfg,
                          const FusedLaunch &L, cudaStream_t s);
-const char *fused_kernel_name(int op);
+const char *fused_kernel_name(int op, int precision, const FusedConfig &cfg);
+
+// double-float TMA passes of operators 1 and 8 (fused_df_tma.cu)
+template <int OP>
+cudaError_t launch_fused_df_tma(const Geom &g, const FusedConfig &cfg, const FusedLaunch &L, cudaStream_t s);
 
 // per-(op, type) launchers defined in the fused_*.cu instantiation files
 template <int OP, class T, bool COMP>

@@ -753,17 +753,11 @@ __global__ void __launch_bounds__(NTX *NTY)
                                                       threadIdx.y, smraw, &maps);
 }
 
-template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX, bool TMA, bool SRC = false>
-cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
-  using S = FusedShape<OP, T, COMP, TT, NTX, NTY, CY, VX, TMA>;
-  constexpr int R = S::R, BX = S::BX, BY = S::BY;
-  void *kern;
-  if constexpr (TMA) kern = (void *)fused_pass_tma<OP, T, COMP, TT, NTX, NTY, CY, VX>;
-  else kern = (void *)fused_pass<OP, T, COMP, TT, NTX, NTY, CY, VX, SRC>;
-  const size_t smem = S::smem_bytes;
-  // the shared-memory opt-in is a function attribute of each device: set it once
-  // per (instantiation, device), from any host thread
-  static std::atomic<unsigned long long> attr_set{0};
+// Prepare a fused kernel for launch on the current device: opt in to its
+// dynamic shared memory (a function attribute of each device, set once per
+// (kernel, device) from any host thread) and return its resident CTAs per SM.
+inline cudaError_t fused_kernel_setup(const void *kern, size_t smem, int threads,
+                                      std::atomic<unsigned long long> &attr_set, int *occ_out, int *nsm_out) {
   int dev = 0;
   cudaGetDevice(&dev);
   const unsigned long long dev_bit = 1ull << (dev & 63);
@@ -773,15 +767,18 @@ cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
     attr_set.fetch_or(dev_bit, std::memory_order_release);
   }
   int occ = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, NTX * NTY, smem);
-  if (occ < 1) occ = 1;
-  const int gx = (g.nx + BX - 1) / BX, gy = (g.ny + BY - 1) / BY;
-  const int64_t tiles = (int64_t)gx * gy;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, smem);
+  *occ_out = occ < 1 ? 1 : occ;
   int nsm = 152;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const int64_t cap = (int64_t)nsm * occ;
-  // choose the number of z chunks: minimise waves x (chunk + pipeline overhead)
-  const int over = TT * R + TT * (R + 1);
+  *nsm_out = nsm;
+  return cudaSuccess;
+}
+
+// z chunk length of a fused pass: split the z range so that waves x (chunk +
+// pipeline overhead `over` planes) is smallest over `tiles` x-y tiles and `cap`
+// resident CTAs.
+inline int fused_zchunk(const Geom &g, int64_t tiles, int64_t cap, int over) {
   int best_n = 1;
   double best_cost = 1e300;
   for (int n = 1; n <= 64 && n <= g.nz; n++) {
@@ -794,9 +791,11 @@ cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
       best_n = n;
     }
   }
-  const int zchunk = (g.nz + best_n - 1) / best_n;
-  const int nz_ch = (g.nz + zchunk - 1) / zchunk;
-  using ST = typename StorageOf<T>::type;
+  return (g.nz + best_n - 1) / best_n;
+}
+
+// Kernel arguments of one fused pass.
+template <class ST> FusedArgs<ST> make_fused_args(const Geom &g, const FusedLaunch &L, int zchunk) {
   FusedArgs<ST> a{};
   a.g = g;
   a.prev = static_cast<const ST *>(L.prev);
@@ -817,6 +816,26 @@ cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
   a.cov_cur = L.cov_cur;
   a.zchunk = zchunk;
   a.write_prev = L.write_prev;
+  return a;
+}
+
+template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX, bool TMA, bool SRC = false>
+cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
+  using S = FusedShape<OP, T, COMP, TT, NTX, NTY, CY, VX, TMA>;
+  constexpr int R = S::R, BX = S::BX, BY = S::BY;
+  void *kern;
+  if constexpr (TMA) kern = (void *)fused_pass_tma<OP, T, COMP, TT, NTX, NTY, CY, VX>;
+  else kern = (void *)fused_pass<OP, T, COMP, TT, NTX, NTY, CY, VX, SRC>;
+  const size_t smem = S::smem_bytes;
+  static std::atomic<unsigned long long> attr_set{0};
+  int occ = 1, nsm = 152;
+  cudaError_t e = fused_kernel_setup(kern, smem, NTX * NTY, attr_set, &occ, &nsm);
+  if (e != cudaSuccess) return e;
+  const int gx = (g.nx + BX - 1) / BX, gy = (g.ny + BY - 1) / BY;
+  const int zchunk = fused_zchunk(g, (int64_t)gx * gy, (int64_t)nsm * occ, TT * R + TT * (R + 1));
+  const int nz_ch = (g.nz + zchunk - 1) / zchunk;
+  using ST = typename StorageOf<T>::type;
+  FusedArgs<ST> a = make_fused_args<ST>(g, L, zchunk);
   if constexpr (TMA) {
     if (!L.tma_cur || !L.tma_roc2 || !L.tma_prev) return cudaErrorInvalidValue;
     // the copies must fill exactly the ring slots this shape sizes
@@ -878,6 +897,10 @@ cudaError_t launch_fused_op_impl(const Geom &g, const FusedConfig &cfg, const Fu
         break;
       case 4:  // x pairs: 32 x 64 region, 1024 threads (radius 1)
         if constexpr (OpTraits<OP>::R == 1) return launch_variant<OP, T, COMP, 16, 64, 1, 2, TM>(g, L, s);
+        break;
+      case 5:  // TMA-staged 32 x 32 and 32 x 64 regions (fused_df_tma.cu)
+      case 6:
+        if constexpr (OP == 1 || OP == 8) return launch_fused_df_tma<OP>(g, cfg, L, s);
         break;
     }
   } else if constexpr (OpTraits<OP>::R == 1) {  // x pairs: vector loads, stores and shared-memory traffic

@@ -278,11 +278,14 @@ EncodeTiledFn encode_tiled() {
 }
 
 const CUtensorMap *tensor_map(girih_gpu_ctx *c, int arr, const void *base) {
-  const int v = c->fcfg.variant - 2;
+  // one cache slot per TMA variant of the context's precision: 2 and 3 (FP32
+  // storage) or the double-float 5 and 6
+  const int v = c->fcfg.variant >= 5 ? c->fcfg.variant - 5 : c->fcfg.variant - 2;
   if (v < 0 || v > 1) return nullptr;
-  // re-encode when the box changed: a TMA copy of another width would overrun
-  // (or under-fill) the ring slots the kernel sized for its own region
-  if (!c->tmap_ok[arr][v] || c->tmap_box[arr][v][0] != c->fcfg.box_w || c->tmap_box[arr][v][1] != c->fcfg.box_h) {
+  // re-encode when the box or the array changed: a TMA copy of another width
+  // would overrun (or under-fill) the ring slots the kernel sized for its own region
+  if (!c->tmap_ok[arr][v] || c->tmap_box[arr][v][0] != c->fcfg.box_w || c->tmap_box[arr][v][1] != c->fcfg.box_h ||
+      c->tmap_base[arr][v] != base) {
     c->tmap_ok[arr][v] = false;
     EncodeTiledFn fn = encode_tiled();
     if (!fn) return nullptr;
@@ -298,6 +301,7 @@ const CUtensorMap *tensor_map(girih_gpu_ctx *c, int arr, const void *base) {
     c->tmap_ok[arr][v] = true;
     c->tmap_box[arr][v][0] = c->fcfg.box_w;
     c->tmap_box[arr][v][1] = c->fcfg.box_h;
+    c->tmap_base[arr][v] = base;
   }
   return &c->tmaps[arr][v];
 }
@@ -427,9 +431,9 @@ int issue_steps_impl(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *
       L.src_n = c->src_n;
     }
     if (c->fcfg.box_w > 0) {  // TMA variant
-      L.tma_prev = tensor_map(c, *iu1, c->f[*iu1]);
-      L.tma_cur = tensor_map(c, *iu2, c->f[*iu2]);
-      L.tma_roc2 = c->g.to == 2 ? tensor_map(c, 4, c->roc2) : L.tma_cur;
+      L.tma_prev = tensor_map(c, *iu1, buf[*iu1]);
+      L.tma_cur = tensor_map(c, *iu2, buf[*iu2]);
+      L.tma_roc2 = c->g.to == 2 ? tensor_map(c, 4, dfp ? c->dfr2 : c->roc2) : L.tma_cur;
       L.tma_box_w = c->fcfg.box_w;
       L.tma_box_h = c->fcfg.box_h;
       if (!L.tma_prev || !L.tma_cur || !L.tma_roc2)
@@ -983,7 +987,7 @@ int girih_gpu_info(girih_gpu_ctx *c, girih_gpu_info_t *info) {
   info->bytes_per_lup = bytes;
   info->device_bytes = c->dev_bytes;
   std::snprintf(info->kernel_name, sizeof(info->kernel_name), "%s",
-                c->sched == GIRIH_SCHED_FUSED ? fused_kernel_name(g.op) : plain_kernel_name(g.op));
+                c->sched == GIRIH_SCHED_FUSED ? fused_kernel_name(g.op, c->d.precision, c->fcfg) : plain_kernel_name(g.op));
   return 0;
 }
 

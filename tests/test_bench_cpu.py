@@ -148,7 +148,7 @@ def test_measured_peak_is_read_from_the_driver_file():
 
 
 def test_committed_traffic_is_per_launch_bytes():
-    t = bench.committed_traffic("fused_pass:star7_leapfrog_512:mixed")
+    t = bench.committed_traffic("fused_pass_tma:star7_leapfrog_512:mixed")
     algorithmic = 20 * 514 ** 3  # one depth-4 pass over the 512^3 grid with its halo
     assert t is not None and 1.0 <= t / algorithmic < 1.2
     assert np.isfinite(t)

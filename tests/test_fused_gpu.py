@@ -190,6 +190,39 @@ def test_fused_double_float_within_fp64_bound(op, variant):
         np.testing.assert_array_equal(u1[:, :, :r], g0.U1[:, :, :r])
 
 
+@pytest.mark.parametrize("op", [1, 8])
+@pytest.mark.parametrize("variant", [5, 6])
+def test_fused_double_float_tma_equals_register_kernel(op, variant):
+    """The TMA-staged double-float kernel (variants 5 and 6: 32-row regions of
+    32 and 64 columns, two adjacent rows per thread) performs the register
+    kernel's arithmetic in the same order: results bit-identical to variant 2
+    (64 x 16 region, another tiling) at both depths, with odd nt (a final pass
+    of depth 1), grids smaller than one box, boxes over every domain edge, and
+    several z chunks; held to the FP64 bound against the oracle."""
+    cols = 32 if variant == 5 else 64
+    for shape in ((45, 38, 29), (5, 3, 4), (70, 2, 9), (97, 130, 67)):
+        g0 = oracle_grid(op, *shape, seed=29)
+        nt = 9
+        ref = g0.copy().run(nt, nthreads=4)
+        for depth in (1, 2):
+            # boxes start on 16 bytes (2 columns): the aligned width at depth 2, the general one at depth 1
+            block = (cols - 2 * depth - (depth % 2), 32 - 2 * depth)
+            with gpu_context(g0.copy(), precision="fp64df", schedule="fused", fusion_depth=depth,
+                             block=block) as ctx, \
+                    gpu_context(g0.copy(), precision="fp64df", schedule="fused", fusion_depth=depth,
+                                block=(64 - 2 * depth, 16 - 2 * depth)) as reg:
+                assert ctx.info()["kernel_name"] == "fused_df_tma"
+                assert reg.info()["kernel_name"] == "fused_pass"
+                ctx.run(nt)
+                reg.run(nt)
+                u1, u2 = ctx.download()
+                r1, r2 = reg.download()
+            np.testing.assert_array_equal(u1, r1)
+            np.testing.assert_array_equal(u2, r2)
+            assert max_rel(u1, ref.U1, ref) <= FP64_TOL
+            assert max_rel(u2, ref.U2, ref) <= FP64_TOL
+
+
 def test_fused_double_float_reference_init():
     """The reference ramp + 100.1 boundary sources (operator 1, default coefficients)."""
     g0 = oracle_grid(1, 45, 31, 27)

@@ -117,9 +117,14 @@ __global__ void __launch_bounds__(kBX *kBY) plain_step_quad(StepArgs<T> a, int z
 #pragma unroll
   for (int m = 0; m < 5; m++) cc[m] = a.cc[m];
   T q[2 * R + 1][VX];
+  // Loads: the normal build addresses every vector as a.v + c +/- offset (with
+  // the negative offsets written as subtractions: the radius-4 kernel then
+  // compiles to 76 registers, three CTAs per SM, against 90-127 for other
+  // spellings of the same addresses); the checked build first tests each
+  // vector range against the array and skips a load outside it (values zero).
+#if GIRIH_CHECKED
   unsigned *const flag = a.flag;
   const int64_t n = a.g.elems;
-  // checked build: each vector access range inside the array (a load outside is skipped)
   auto ld = [&](int64_t off, T(&e)[VX]) {
     if (in_array(off, VX, n, flag)) {
       vload<T, VX>(a.v + off, e);
@@ -128,20 +133,30 @@ __global__ void __launch_bounds__(kBX *kBY) plain_step_quad(StepArgs<T> a, int z
       for (int v = 0; v < VX; v++) e[v] = T(0);
     }
   };
+#define GIRIH_QLD(off, e) ld(c + (off), e)
+#define GIRIH_QLD_M(off, e) ld(c - (off), e)
+#else
+#define GIRIH_QLD(off, e) vload<T, VX>(a.v + c + (off), e)
+#define GIRIH_QLD_M(off, e) vload<T, VX>(a.v + c - (off), e)
+#endif
 #pragma unroll
-  for (int d = 0; d < 2 * R; d++) ld(c + (int64_t)(d - R) * plane, q[d]);
+  for (int d = 0; d < 2 * R; d++) GIRIH_QLD((int64_t)(d - R) * plane, q[d]);
   const bool full = i0 + VX <= a.g.nx;
   for (int k = k0; k < k1; k++, c += plane) {
-    ld(c + (int64_t)R * plane, q[2 * R]);
+    GIRIH_QLD((int64_t)R * plane, q[2 * R]);
     T xl[VX], xr[VX], yv[2 * R][VX];
-    ld(c - VX, xl);
-    ld(c + VX, xr);
+    GIRIH_QLD_M(VX, xl);
+    GIRIH_QLD(VX, xr);
 #pragma unroll
     for (int d = 1; d <= R; d++) {
-      ld(c + d * px, yv[d - 1]);
-      ld(c - d * px, yv[R + d - 1]);
+      GIRIH_QLD(d * px, yv[d - 1]);
+      GIRIH_QLD_M(d * px, yv[R + d - 1]);
     }
+#undef GIRIH_QLD
+#undef GIRIH_QLD_M
+#if GIRIH_CHECKED
     if (!in_array(c, VX, n, flag)) continue;  // the old value, roc2, coefficients and the store
+#endif
     T uo[VX], r2[VX];
     if constexpr (TO == 2) {
       VecU<T, VX> u;

@@ -266,13 +266,17 @@ struct FusedShape {
   static constexpr size_t smem_bytes = TMA ? off_bar + NB * sizeof(uint64_t) : field_bytes;
 };
 
-// One CTA-tile of a fused pass: tile (bxi, byi) of the x-y tiling, z chunk bzi,
+// One CTA-tile of a fused pass: tile (bxi, byi) of the x-y tiling, z chunk bzi
+// (planes [R + bzi*zchunk, ...)), or, with zlo >= 0, planes [zlo, zhi),
 // executed by the NTX*NTY threads of the calling CTA (thread (tx, ty)).  Used by
-// the single-grid kernel below and by the batched persistent kernel.
+// the single-grid persistent kernels below (one call per piece of work; `first`
+// on the CTA's first, later calls re-initialise the TMA barriers) and by the
+// batched persistent kernel.
 template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX, bool TMA = false, bool SRC = false>
 __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>::type> &a, int bxi, int byi,
                                            int bzi, int tx, int ty, unsigned char *smraw,
-                                           const TmaMaps *maps = nullptr) {
+                                           const TmaMaps *maps = nullptr, int zlo = -1, int zhi = -1,
+                                           bool first = true) {
   using Sh = FusedShape<OP, T, COMP, TT, NTX, NTY, CY, VX, TMA>;
   using ST = typename StorageOf<T>::type;
   constexpr int R = Sh::R, TO = Sh::TO, D = Sh::D, QL = Sh::QL, U = Sh::U;
@@ -294,8 +298,8 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
   // grids of fewer than 2^31 elements per array
   const int plane = (int)g.plane;
   const int X0 = bxi * BX, Y0 = byi * BY;
-  const int Z0 = R + bzi * a.zchunk;
-  const int Z1 = min(Z0 + a.zchunk, g.nnz - R);
+  const int Z0 = zlo >= 0 ? zlo : R + bzi * a.zchunk;
+  const int Z1 = zlo >= 0 ? zhi : min(Z0 + a.zchunk, g.nnz - R);
   const int sb = max(0, Z0 - H);
   const int se = Z1 - 1 + TT * D;
   const int s0 = sb - sb % U;  // plane p lives in queue slot p mod QL; buffer parity = PH parity
@@ -401,8 +405,11 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
     }
   };
   if constexpr (TMA) {
-    if (tid == 0) {
-      for (int k = 0; k < NB; k++) mbar_init(&bars[k], 1);
+    if (tid == 0) {  // every phase restarts at 0; a barrier of an earlier piece is invalidated first
+      for (int k = 0; k < NB; k++) {
+        if (!first) mbar_inval(&bars[k]);
+        mbar_init(&bars[k], 1);
+      }
       mbar_init_fence();
     }
     __syncthreads();
@@ -736,21 +743,75 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
   }
 }
 
+// Persistent single-grid pass: CTA b takes the work items [b*W, (b+1)*W) of the
+// sequence (tile, plane), planes fastest, W = a.zchunk, one fused_tile call per
+// tile it touches.  Each piece pays the z pipeline's fill and drain (TT*R +
+// TT*D planes) once, against once per z chunk of a (tile, chunk) grid, and
+// every SM stays busy to the end of the pass.
+template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX, bool TMA, bool SRC>
+__device__ __forceinline__ void fused_pieces(const FusedArgs<typename StorageOf<T>::type> &a, unsigned char *smraw,
+                                             const TmaMaps *maps) {
+  using Sh = FusedShape<OP, T, COMP, TT, NTX, NTY, CY, VX, TMA>;
+  const Geom &g = a.g;
+  // 32-bit work indices: tiles x planes <= points < 2^31 (fused_supported)
+  const int gx = (g.nx + Sh::BX - 1) / Sh::BX, gy = (g.ny + Sh::BY - 1) / Sh::BY;
+  const int w0 = blockIdx.x * a.zchunk, w1 = min(gx * gy * g.nz, w0 + a.zchunk);
+  for (int w = w0; w < w1;) {
+    const int t = w / g.nz, za = w - t * g.nz, zb = min(g.nz, za + (w1 - w));
+    fused_tile<OP, T, COMP, TT, NTX, NTY, CY, VX, TMA, SRC>(a, t % gx, t / gx, 0, threadIdx.x, threadIdx.y, smraw,
+                                                           maps, Sh::R + za, Sh::R + zb, w == w0);
+    w += zb - za;
+  }
+}
+
 template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX, bool SRC = false>
 __global__ void __launch_bounds__(NTX *NTY) fused_pass(FusedArgs<typename StorageOf<T>::type> a) {
   extern __shared__ __align__(128) unsigned char smraw[];
-  fused_tile<OP, T, COMP, TT, NTX, NTY, CY, VX, false, SRC>(a, blockIdx.x, blockIdx.y, blockIdx.z, threadIdx.x,
-                                                            threadIdx.y, smraw);
+  fused_pieces<OP, T, COMP, TT, NTX, NTY, CY, VX, false, SRC>(a, smraw, nullptr);
 }
 
 // The same pass with the input planes staged by TMA; the tensor maps travel as
-// grid constants.
+// grid constants.  This one keeps a grid of (tile, z chunk) CTAs, x fastest:
+// the CTAs running at one time are neighbouring tiles at the same z, whose
+// overlapping halo boxes then come from L2 (the persistent order above ran
+// the 512^3 mixed leapfrog at 451 against 550 GLUP/s).
 template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX>
 __global__ void __launch_bounds__(NTX *NTY)
     fused_pass_tma(FusedArgs<typename StorageOf<T>::type> a, const __grid_constant__ TmaMaps maps) {
   extern __shared__ __align__(128) unsigned char smraw[];
   fused_tile<OP, T, COMP, TT, NTX, NTY, CY, VX, true>(a, blockIdx.x, blockIdx.y, blockIdx.z, threadIdx.x,
                                                       threadIdx.y, smraw, &maps);
+}
+
+// Work per CTA of a persistent pass over `tiles` x-y tiles and nz planes with
+// `cap` resident CTAs: the makespan is about the work of one CTA plus one
+// pipeline fill per piece, so every resident slot gets work (at least one
+// plane); *ctas receives the grid.
+inline int fused_pieces_per_cta(const Geom &g, int64_t tiles, int64_t cap, int64_t *ctas) {
+  const int64_t total = tiles * g.nz;
+  const int64_t n = std::max<int64_t>(1, std::min<int64_t>(cap, total));
+  const int64_t per = (total + n - 1) / n;
+  *ctas = (total + per - 1) / per;
+  return (int)per;
+}
+
+// z chunk length of a (tile, z chunk) grid: split the z range so that waves x
+// (chunk + pipeline overhead `over` planes) is smallest over `tiles` x-y tiles
+// and `cap` resident CTAs.
+inline int fused_zchunk(const Geom &g, int64_t tiles, int64_t cap, int over) {
+  int best_n = 1;
+  double best_cost = 1e300;
+  for (int n = 1; n <= 64 && n <= g.nz; n++) {
+    int chunk = (g.nz + n - 1) / n;
+    int64_t ctas = tiles * n;
+    int64_t waves = (ctas + cap - 1) / cap;
+    double cost = (double)waves * (chunk + over);
+    if (cost < best_cost * 0.999) {
+      best_cost = cost;
+      best_n = n;
+    }
+  }
+  return (g.nz + best_n - 1) / best_n;
 }
 
 // Prepare a fused kernel for launch on the current device: opt in to its
@@ -773,25 +834,6 @@ inline cudaError_t fused_kernel_setup(const void *kern, size_t smem, int threads
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   *nsm_out = nsm;
   return cudaSuccess;
-}
-
-// z chunk length of a fused pass: split the z range so that waves x (chunk +
-// pipeline overhead `over` planes) is smallest over `tiles` x-y tiles and `cap`
-// resident CTAs.
-inline int fused_zchunk(const Geom &g, int64_t tiles, int64_t cap, int over) {
-  int best_n = 1;
-  double best_cost = 1e300;
-  for (int n = 1; n <= 64 && n <= g.nz; n++) {
-    int chunk = (g.nz + n - 1) / n;
-    int64_t ctas = tiles * n;
-    int64_t waves = (ctas + cap - 1) / cap;
-    double cost = (double)waves * (chunk + over);
-    if (cost < best_cost * 0.999) {
-      best_cost = cost;
-      best_n = n;
-    }
-  }
-  return (g.nz + best_n - 1) / best_n;
 }
 
 // Kernel arguments of one fused pass.
@@ -832,8 +874,14 @@ cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
   cudaError_t e = fused_kernel_setup(kern, smem, NTX * NTY, attr_set, &occ, &nsm);
   if (e != cudaSuccess) return e;
   const int gx = (g.nx + BX - 1) / BX, gy = (g.ny + BY - 1) / BY;
-  const int zchunk = fused_zchunk(g, (int64_t)gx * gy, (int64_t)nsm * occ, TT * R + TT * (R + 1));
-  const int nz_ch = (g.nz + zchunk - 1) / zchunk;
+  int64_t ctas = 1;
+  int zchunk = 1, nz_ch = 1;
+  if constexpr (TMA) {
+    zchunk = fused_zchunk(g, (int64_t)gx * gy, (int64_t)nsm * occ, TT * R + TT * (R + 1));
+    nz_ch = (g.nz + zchunk - 1) / zchunk;
+  } else {
+    zchunk = fused_pieces_per_cta(g, (int64_t)gx * gy, (int64_t)nsm * occ, &ctas);
+  }
   using ST = typename StorageOf<T>::type;
   FusedArgs<ST> a = make_fused_args<ST>(g, L, zchunk);
   if constexpr (TMA) {
@@ -846,7 +894,7 @@ cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
     maps.roc2 = *static_cast<const CUtensorMap *>(L.tma_roc2);
     fused_pass_tma<OP, T, COMP, TT, NTX, NTY, CY, VX><<<dim3(gx, gy, nz_ch), dim3(NTX, NTY), smem, s>>>(a, maps);
   } else {
-    fused_pass<OP, T, COMP, TT, NTX, NTY, CY, VX, SRC><<<dim3(gx, gy, nz_ch), dim3(NTX, NTY), smem, s>>>(a);
+    fused_pass<OP, T, COMP, TT, NTX, NTY, CY, VX, SRC><<<(unsigned)ctas, dim3(NTX, NTY), smem, s>>>(a);
   }
   return cudaGetLastError();
 }

@@ -245,26 +245,20 @@ __device__ __forceinline__ unsigned df_tma_piece(const FusedArgs<Df64> &a, const
   return timeout;
 }
 
-// Persistent pass: CTA b takes the work items [b*W, (b+1)*W) of the sequence
-// (tile, plane) with planes fastest, W = a.zchunk, as one piece per tile it
-// touches.  A piece pays the z pipeline's fill and drain (~TT*D + TT planes)
-// once, against once per z chunk of a grid of (tile, chunk) CTAs, and every
-// SM stays busy to the end.
+// Persistent pass: the pieces of for_each_piece (whole tiles while every CTA
+// can take one, then the remaining tiles' planes split evenly), each paying
+// the z pipeline's fill (~TT*D + TT planes) once.
 template <int OP, int TT, int NTX, int NTY>
 __global__ void __launch_bounds__(NTX *NTY, NTX * NTY <= 512 ? 2 : 1)
     fused_df_tma(FusedArgs<Df64> a, const __grid_constant__ TmaMaps maps) {
   using S = DfTmaShape<OP, TT, NTX, NTY>;
   extern __shared__ __align__(128) unsigned char smraw[];
   const Geom &g = a.g;
-  // 32-bit work indices: tiles x planes <= points < 2^31 (fused_supported)
-  const int gx = (g.nx + S::BX - 1) / S::BX, gy = (g.ny + S::BY - 1) / S::BY;
-  const int w0 = blockIdx.x * a.zchunk, w1 = min(gx * gy * g.nz, w0 + a.zchunk);
   unsigned timeout = 0;
-  for (int w = w0; w < w1;) {
-    const int t = w / g.nz, za = w - t * g.nz, zb = min(g.nz, za + (w1 - w));
-    timeout |= df_tma_piece<OP, TT, NTX, NTY>(a, maps, t % gx, t / gx, S::R + za, S::R + zb, w == w0, smraw);
-    w += zb - za;
-  }
+  for_each_piece((g.nx + S::BX - 1) / S::BX, (g.ny + S::BY - 1) / S::BY, g.nz,
+                 [&](int bxi, int byi, int za, int zb, bool first) {
+                   timeout |= df_tma_piece<OP, TT, NTX, NTY>(a, maps, bxi, byi, S::R + za, S::R + zb, first, smraw);
+                 });
   if (timeout && a.range_flag) atomicOr(a.range_flag, 2u);  // a copy never completed within the wait bound
 }
 
@@ -279,13 +273,10 @@ cudaError_t launch_df_tma_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s
   if (!L.tma_cur || !L.tma_prev || !L.tma_roc2) return cudaErrorInvalidValue;
   // the copies must fill exactly the ring slots this shape sizes
   if (L.tma_box_w != S::RW || L.tma_box_h != S::RY) return cudaErrorInvalidValue;
-  // persistent grid: one CTA per resident slot (the kernel is issue-bound, so
-  // the halo boxes it re-reads from DRAM instead of L2 cost less than the
-  // pipeline fills of a (tile, z chunk) grid: 218 against 202 GLUP/s at 512^3)
+  // persistent grid: one CTA per resident slot
   const int gx = (g.nx + S::BX - 1) / S::BX, gy = (g.ny + S::BY - 1) / S::BY;
-  int64_t ctas = 1;
-  const int per = fused_pieces_per_cta(g, (int64_t)gx * gy, (int64_t)nsm * occ, &ctas);
-  FusedArgs<Df64> a = make_fused_args<Df64>(g, L, per);
+  const int64_t ctas = fused_persistent_ctas(g, (int64_t)gx * gy, (int64_t)nsm * occ);
+  FusedArgs<Df64> a = make_fused_args<Df64>(g, L, 0);
   TmaMaps maps;
   maps.cur = *static_cast<const CUtensorMap *>(L.tma_cur);
   maps.prev = *static_cast<const CUtensorMap *>(L.tma_prev);

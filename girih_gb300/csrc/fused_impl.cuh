@@ -743,25 +743,49 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
   }
 }
 
-// Persistent single-grid pass: CTA b takes the work items [b*W, (b+1)*W) of the
-// sequence (tile, plane), planes fastest, W = a.zchunk, one fused_tile call per
-// tile it touches.  Each piece pays the z pipeline's fill and drain (TT*R +
-// TT*D planes) once, against once per z chunk of a (tile, chunk) grid, and
-// every SM stays busy to the end of the pass.
+// Persistent schedule of a single-grid pass over gx*gy tiles (row-major) and
+// nz planes on gridDim.x CTAs, as pieces (tile, planes [za, zb)) handed to
+// f(bxi, byi, za, zb, first):
+//   phase 1: CTA b takes whole tiles b, b + C, b + 2C, ... (C = gridDim.x) while
+//     C of them remain, so that all CTAs stream the same planes at the same time
+//     and neighbouring tiles share their overlapping halo boxes in L2;
+//   phase 2: the remaining tiles' planes are split evenly over all CTAs, tile by
+//     tile, so that CTAs b and b + C/remaining hold neighbouring tiles over the
+//     same planes.
+// Each piece pays the z pipeline's fill once (against once per z chunk of a
+// (tile, chunk) grid) and every SM works to the end of the pass.  32-bit work
+// indices: tiles x planes <= points < 2^31 (fused_supported).
+template <class F> __device__ __forceinline__ void for_each_piece(int gx, int gy, int nz, F &&f) {
+  const int tiles = gx * gy, C = gridDim.x, b = blockIdx.x;
+  const int full = tiles / C;
+  bool first = true;
+  for (int r = 0; r < full; r++) {
+    const int t = r * C + b;
+    f(t % gx, t / gx, 0, nz, first);
+    first = false;
+  }
+  const int rest = tiles - full * C;
+  if (rest == 0) return;
+  const int work = rest * nz, per = (work + C - 1) / C;
+  const int w1 = min(work, (b + 1) * per);
+  for (int w = b * per; w < w1;) {
+    const int t = full * C + w / nz, za = w % nz, zb = min(nz, za + (w1 - w));
+    f(t % gx, t / gx, za, zb, first);
+    first = false;
+    w += zb - za;
+  }
+}
+
 template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX, bool TMA, bool SRC>
 __device__ __forceinline__ void fused_pieces(const FusedArgs<typename StorageOf<T>::type> &a, unsigned char *smraw,
                                              const TmaMaps *maps) {
   using Sh = FusedShape<OP, T, COMP, TT, NTX, NTY, CY, VX, TMA>;
   const Geom &g = a.g;
-  // 32-bit work indices: tiles x planes <= points < 2^31 (fused_supported)
-  const int gx = (g.nx + Sh::BX - 1) / Sh::BX, gy = (g.ny + Sh::BY - 1) / Sh::BY;
-  const int w0 = blockIdx.x * a.zchunk, w1 = min(gx * gy * g.nz, w0 + a.zchunk);
-  for (int w = w0; w < w1;) {
-    const int t = w / g.nz, za = w - t * g.nz, zb = min(g.nz, za + (w1 - w));
-    fused_tile<OP, T, COMP, TT, NTX, NTY, CY, VX, TMA, SRC>(a, t % gx, t / gx, 0, threadIdx.x, threadIdx.y, smraw,
-                                                           maps, Sh::R + za, Sh::R + zb, w == w0);
-    w += zb - za;
-  }
+  for_each_piece((g.nx + Sh::BX - 1) / Sh::BX, (g.ny + Sh::BY - 1) / Sh::BY, g.nz,
+                 [&](int bxi, int byi, int za, int zb, bool first) {
+                   fused_tile<OP, T, COMP, TT, NTX, NTY, CY, VX, TMA, SRC>(a, bxi, byi, 0, threadIdx.x, threadIdx.y,
+                                                                          smraw, maps, Sh::R + za, Sh::R + zb, first);
+                 });
 }
 
 template <int OP, class T, bool COMP, int TT, int NTX, int NTY, int CY, int VX, bool SRC = false>
@@ -783,16 +807,11 @@ __global__ void __launch_bounds__(NTX *NTY)
                                                       threadIdx.y, smraw, &maps);
 }
 
-// Work per CTA of a persistent pass over `tiles` x-y tiles and nz planes with
-// `cap` resident CTAs: the makespan is about the work of one CTA plus one
-// pipeline fill per piece, so every resident slot gets work (at least one
-// plane); *ctas receives the grid.
-inline int fused_pieces_per_cta(const Geom &g, int64_t tiles, int64_t cap, int64_t *ctas) {
-  const int64_t total = tiles * g.nz;
-  const int64_t n = std::max<int64_t>(1, std::min<int64_t>(cap, total));
-  const int64_t per = (total + n - 1) / n;
-  *ctas = (total + per - 1) / per;
-  return (int)per;
+// CTAs of a persistent pass (for_each_piece) over `tiles` x-y tiles and nz
+// planes with `cap` resident CTAs: every resident slot, as long as each gets
+// at least one plane.
+inline int64_t fused_persistent_ctas(const Geom &g, int64_t tiles, int64_t cap) {
+  return std::max<int64_t>(1, std::min<int64_t>(cap, tiles * g.nz));
 }
 
 // z chunk length of a (tile, z chunk) grid: split the z range so that waves x
@@ -880,7 +899,7 @@ cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
     zchunk = fused_zchunk(g, (int64_t)gx * gy, (int64_t)nsm * occ, TT * R + TT * (R + 1));
     nz_ch = (g.nz + zchunk - 1) / zchunk;
   } else {
-    zchunk = fused_pieces_per_cta(g, (int64_t)gx * gy, (int64_t)nsm * occ, &ctas);
+    ctas = fused_persistent_ctas(g, (int64_t)gx * gy, (int64_t)nsm * occ);
   }
   using ST = typename StorageOf<T>::type;
   FusedArgs<ST> a = make_fused_args<ST>(g, L, zchunk);

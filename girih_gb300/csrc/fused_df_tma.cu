@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(NTX *NTY, NTX * NTY <= 512 ? 2 : 1)
   extern __shared__ __align__(128) unsigned char smraw[];
   const Geom &g = a.g;
   unsigned timeout = 0;
-  for_each_piece((g.nx + S::BX - 1) / S::BX, (g.ny + S::BY - 1) / S::BY, g.nz,
+  for_each_piece((g.nx + S::BX - 1) / S::BX, (g.ny + S::BY - 1) / S::BY, g.nz, a.zchunk,
                  [&](int bxi, int byi, int za, int zb, bool first) {
                    timeout |= df_tma_piece<OP, TT, NTX, NTY>(a, maps, bxi, byi, S::R + za, S::R + zb, first, smraw);
                  });
@@ -276,7 +276,8 @@ cudaError_t launch_df_tma_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s
   // persistent grid: one CTA per resident slot
   const int gx = (g.nx + S::BX - 1) / S::BX, gy = (g.ny + S::BY - 1) / S::BY;
   const int64_t ctas = fused_persistent_ctas(g, (int64_t)gx * gy, (int64_t)nsm * occ);
-  FusedArgs<Df64> a = make_fused_args<Df64>(g, L, 0);
+  const int parts = fused_phase2_parts((int64_t)gx * gy, ctas, g.nz, TT * S::R + TT * S::D);
+  FusedArgs<Df64> a = make_fused_args<Df64>(g, L, parts);
   TmaMaps maps;
   maps.cur = *static_cast<const CUtensorMap *>(L.tma_cur);
   maps.prev = *static_cast<const CUtensorMap *>(L.tma_prev);

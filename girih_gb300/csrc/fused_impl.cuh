@@ -20,6 +20,7 @@
 #pragma once
 #include <algorithm>
 #include <atomic>
+#include <cstdint>
 #include <type_traits>
 #include <utility>
 
@@ -41,7 +42,7 @@ template <class S> struct FusedArgs {
   S *out_prev, *out_cur;
   double cc[5];
   float cch[5], ccl[5];  // cc split on the host: hi = nearest FP32, lo = nearest FP32 of the rest
-  int zchunk;
+  int zchunk;      // z chunk of a (tile, chunk) grid; plane split k of a persistent one (for_each_piece)
   int write_prev;
   unsigned *range_flag;  // error flags (bit 1: a TMA copy timed out)
   const void *coef;      // variable coefficients: nc arrays of g.elems (S, or BF16 in the mixed form)
@@ -749,13 +750,16 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
 //   phase 1: CTA b takes whole tiles b, b + C, b + 2C, ... (C = gridDim.x) while
 //     C of them remain, so that all CTAs stream the same planes at the same time
 //     and neighbouring tiles share their overlapping halo boxes in L2;
-//   phase 2: the remaining tiles' planes are split evenly over all CTAs, tile by
-//     tile, so that CTAs b and b + C/remaining hold neighbouring tiles over the
-//     same planes.
+//   phase 2: each of the `rest` remaining tiles is split into k equal plane
+//     ranges (k from fused_phase2_parts), pieces numbered tile by tile and
+//     dealt in rounds of C, so that the pieces of neighbouring tiles over the
+//     same planes run at the same time; the pieces of a last, partial round go
+//     to CTAs spread evenly over the grid (piece q of Q to CTA q*C/Q), not to
+//     the first Q, which the hardware would place on neighbouring SMs.
 // Each piece pays the z pipeline's fill once (against once per z chunk of a
-// (tile, chunk) grid) and every SM works to the end of the pass.  32-bit work
-// indices: tiles x planes <= points < 2^31 (fused_supported).
-template <class F> __device__ __forceinline__ void for_each_piece(int gx, int gy, int nz, F &&f) {
+// (tile, chunk) grid).  32-bit work indices: tiles x planes <= points < 2^31
+// (fused_supported).
+template <class F> __device__ __forceinline__ void for_each_piece(int gx, int gy, int nz, int k, F &&f) {
   const int tiles = gx * gy, C = gridDim.x, b = blockIdx.x;
   const int full = tiles / C;
   bool first = true;
@@ -766,13 +770,16 @@ template <class F> __device__ __forceinline__ void for_each_piece(int gx, int gy
   }
   const int rest = tiles - full * C;
   if (rest == 0) return;
-  const int work = rest * nz, per = (work + C - 1) / C;
-  const int w1 = min(work, (b + 1) * per);
-  for (int w = b * per; w < w1;) {
-    const int t = full * C + w / nz, za = w % nz, zb = min(nz, za + (w1 - w));
-    f(t % gx, t / gx, za, zb, first);
-    first = false;
-    w += zb - za;
+  k = max(1, min(nz, k));
+  const int P = k * rest;
+  for (int base = 0; base < P; base += C) {
+    const int Q = min(C, P - base);
+    const int q = (int)(((int64_t)b * Q + C - 1) / C);  // the one piece q with q*C/Q == b, if any
+    if (q < Q && (int)((int64_t)q * C / Q) == b) {
+      const int p = base + q, t = full * C + p / k, part = p % k;
+      f(t % gx, t / gx, part * nz / k, (part + 1) * nz / k, first);
+      first = false;
+    }
   }
 }
 
@@ -781,7 +788,7 @@ __device__ __forceinline__ void fused_pieces(const FusedArgs<typename StorageOf<
                                              const TmaMaps *maps) {
   using Sh = FusedShape<OP, T, COMP, TT, NTX, NTY, CY, VX, TMA>;
   const Geom &g = a.g;
-  for_each_piece((g.nx + Sh::BX - 1) / Sh::BX, (g.ny + Sh::BY - 1) / Sh::BY, g.nz,
+  for_each_piece((g.nx + Sh::BX - 1) / Sh::BX, (g.ny + Sh::BY - 1) / Sh::BY, g.nz, a.zchunk,
                  [&](int bxi, int byi, int za, int zb, bool first) {
                    fused_tile<OP, T, COMP, TT, NTX, NTY, CY, VX, TMA, SRC>(a, bxi, byi, 0, threadIdx.x, threadIdx.y,
                                                                           smraw, maps, Sh::R + za, Sh::R + zb, first);
@@ -812,6 +819,24 @@ __global__ void __launch_bounds__(NTX *NTY)
 // at least one plane.
 inline int64_t fused_persistent_ctas(const Geom &g, int64_t tiles, int64_t cap) {
   return std::max<int64_t>(1, std::min<int64_t>(cap, tiles * g.nz));
+}
+
+// Plane split k of the tiles left after the whole-tile rounds of a persistent
+// pass on C CTAs: the k (<= 64) with the fewest rounds x (planes per piece +
+// the pipeline's `over` fill planes), the smaller k on a tie.
+inline int fused_phase2_parts(int64_t tiles, int64_t C, int nz, int over) {
+  const int64_t rest = tiles % C;
+  if (rest == 0) return 1;
+  int best_k = 1;
+  int64_t best = INT64_MAX;
+  for (int k = 1; k <= 64 && k <= nz; k++) {
+    const int64_t rounds = (rest * k + C - 1) / C, cost = rounds * ((nz + k - 1) / k + over);
+    if (cost < best) {
+      best = cost;
+      best_k = k;
+    }
+  }
+  return best_k;
 }
 
 // z chunk length of a (tile, z chunk) grid: split the z range so that waves x
@@ -900,6 +925,7 @@ cudaError_t launch_tt(const Geom &g, const FusedLaunch &L, cudaStream_t s) {
     nz_ch = (g.nz + zchunk - 1) / zchunk;
   } else {
     ctas = fused_persistent_ctas(g, (int64_t)gx * gy, (int64_t)nsm * occ);
+    zchunk = fused_phase2_parts((int64_t)gx * gy, ctas, g.nz, TT * R + TT * (R + 1));
   }
   using ST = typename StorageOf<T>::type;
   FusedArgs<ST> a = make_fused_args<ST>(g, L, zchunk);

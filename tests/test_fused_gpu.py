@@ -193,24 +193,25 @@ def test_fused_double_float_within_fp64_bound(op, variant):
 @pytest.mark.parametrize("op", [1, 8])
 @pytest.mark.parametrize("variant", [5, 6])
 def test_fused_double_float_tma_equals_register_kernel(op, variant):
-    """The TMA-staged double-float kernel (variants 5 and 6: 32-row regions of
-    32 and 64 columns, two adjacent rows per thread) performs the register
-    kernel's arithmetic in the same order: results bit-identical to variant 2
-    (64 x 16 region, another tiling) at both depths, with odd nt (a final pass
-    of depth 1), grids smaller than one box, boxes over every domain edge, and
-    several z chunks; held to the FP64 bound against the oracle."""
-    cols = 32 if variant == 5 else 64
+    """The TMA-staged double-float kernel (variants 5 and 6: 32 x 32 and 64 x 32
+    regions, two adjacent rows per thread) performs the register
+    kernel's arithmetic in the same order: results bit-identical to variant 4
+    (32 x 64 region with x pairs in packed f32x2 lanes, another tiling) at both
+    depths, with odd nt (a final pass of depth 1), grids smaller than one box,
+    boxes over every domain edge, and several persistent pieces per CTA; held
+    to the FP64 bound against the oracle."""
+    cols, rows = {5: (32, 32), 6: (64, 32)}[variant]
     for shape in ((45, 38, 29), (5, 3, 4), (70, 2, 9), (97, 130, 67)):
         g0 = oracle_grid(op, *shape, seed=29)
         nt = 9
         ref = g0.copy().run(nt, nthreads=4)
         for depth in (1, 2):
             # boxes start on 16 bytes (2 columns): the aligned width at depth 2, the general one at depth 1
-            block = (cols - 2 * depth - (depth % 2), 32 - 2 * depth)
+            block = (cols - 2 * depth - (depth % 2), rows - 2 * depth)
             with gpu_context(g0.copy(), precision="fp64df", schedule="fused", fusion_depth=depth,
                              block=block) as ctx, \
                     gpu_context(g0.copy(), precision="fp64df", schedule="fused", fusion_depth=depth,
-                                block=(64 - 2 * depth, 16 - 2 * depth)) as reg:
+                                block=(32 - 2 * depth - 1, 64 - 2 * depth)) as reg:
                 assert ctx.info()["kernel_name"] == "fused_df_tma"
                 assert reg.info()["kernel_name"] == "fused_pass"
                 ctx.run(nt)

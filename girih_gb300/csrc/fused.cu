@@ -134,11 +134,14 @@ FusedConfig make_fused_config(const Geom &g, int precision, int depth, int varia
 
 FusedConfig choose_fused_config(const Geom &g, int precision, int depth, int bx, int by) {
   int d = depth;
-  if (d <= 0) d = g.r == 4 ? 2 : (precision == GIRIH_FP64 ? 2 : 4);
+  // untuned: the depth that measured fastest at 512^3 per precision (double-float:
+  // depth 2, the TMA-staged 64 x 32 region first below)
+  if (d <= 0) d = g.r == 4 ? 2 : ((precision == GIRIH_FP64 || precision == GIRIH_FP64_DF) ? 2 : 4);
   d = d > fused_max_depth(g, precision) ? fused_max_depth(g, precision) : d;
-  // double-float: the TMA-staged variants first, so that a tile they share with
-  // a register variant (28 x 28 and 60 x 28 at depth 2) selects them
-  static const int df_order[FV_COUNT] = {5, 6, 0, 1, 2, 3, 4};
+  // double-float: the TMA-staged variants first (the 64 x 32 region, fastest at
+  // 512^3, as the untuned choice), so that a tile they share with a register
+  // variant (28 x 28 and 60 x 28 at depth 2) selects them
+  static const int df_order[FV_COUNT] = {6, 5, 0, 1, 2, 3, 4};
   for (int k = 0; k < FV_COUNT; k++) {
     const int v = precision == GIRIH_FP64_DF ? df_order[k] : k;
     FusedConfig c = make_fused_config(g, precision, d, v);

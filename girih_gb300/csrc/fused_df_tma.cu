@@ -16,7 +16,13 @@
 //     needs no copy into a published plane);
 //   * a thread owns one column and two ADJACENT rows, so one y neighbour of
 //     each row is the other row's register;
-//   * x/y activity and output ownership are bit masks computed once per tile.
+//   * x/y activity and output ownership are bit masks computed once per tile;
+//   * the CTAs are persistent (for_each_piece): whole tiles in rounds, all
+//     CTAs at the same planes so that neighbouring tiles share their halo
+//     boxes in L2, then the remaining tiles split into plane ranges, each piece
+//     paying the z pipeline's fill once.
+// Measured at 512^3 (7-point leapfrog): 132 instead of 152 thread instructions
+// per update, 164 -> 220 GLUP/s.
 //
 // CTA: NTX x NTY threads over a region of NTX columns x 2*NTY rows; the output
 // tile is the region less a halo of TT columns/rows per side (the region start

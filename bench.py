@@ -710,7 +710,7 @@ def run_batched_core(local, nt=100, steps=5, warmup=3, precision="mixed"):
 
 
 def run_batched(args, rank, world, local):
-    """Batched workload line (BASELINE's batched configuration)."""
+    """Batched workload line (64 independent grids of uneven sizes, the batched configuration)."""
     nt = args.nt or 100
     b = run_batched_core(local, nt=nt, steps=args.steps, warmup=args.warmup)
     return {"metric": "GLUP/s, 64 batched grids (7-pt and 25-pt leapfrog, FP32 fields), nt=100",

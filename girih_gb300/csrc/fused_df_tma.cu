@@ -205,7 +205,7 @@ __device__ __forceinline__ unsigned df_tma_piece(const FusedArgs<Df64> &a, const
               else uold = q[L - 2][c][SP];
               // roc2 of plane p arrived with input plane s - (L-1)*D
               const Df64 r2 = lds(ring_roc2 + df_pmod(PH - (L - 1) * D, NR) * PLANE + toff + c * RW);
-              cand = (twice(centre) - uold) + r2 * lap;
+              cand = twice_minus(centre, uold) + r2 * lap;
             } else {
               cand = lap;
             }

@@ -621,7 +621,7 @@ __device__ __forceinline__ void fused_tile(const FusedArgs<typename StorageOf<T>
                 T uold;
                 if constexpr (L >= 2) uold = q[L - 2][c][V][SL];
                 else uold = pvc[c].e[V];
-                cand = (twice(centre) - uold) + r2c[L - 1][c].e[V] * lap;
+                cand = twice_minus(centre, uold) + r2c[L - 1][c].e[V] * lap;
               } else {
                 cand = lap;
               }

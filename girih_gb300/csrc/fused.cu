@@ -75,9 +75,19 @@ static FusedConfig make_box_config(int precision, int depth, int variant) {
 // Double-float radius-1 constant-coefficient operators (1, 8), variants 5 and 6:
 // the TMA-staged kernel of fused_df_tma.cu (32 rows, 32 or 64 columns, depth
 // <= 2).  Its boxes start on 16 bytes (2 columns), so the tile is the aligned
-// width where that loses nothing (depth 2) and the general one else.
+// width where that loses nothing (depth 2) and the general one else.  Operator
+// 0 (radius 4): variant 5 is fused_df_tma4.cu, depth 1, a 32 x 32 tile.
 static FusedConfig make_df_tma_config(const Geom &g, int depth, int variant) {
   FusedConfig c{};
+  if (g.op == 0) {  // radius 4: one step per pass (fused_df_tma4.cu), boxes from an even x
+    if (depth != 1 || variant != 5 || (g.ox & 1)) return c;
+    if (df_tma4_smem() > (size_t)227 * 1024) return c;
+    c.depth = 1;
+    c.variant = 5;
+    c.bx = c.by = df_tma4_tile();
+    c.box_w = c.box_h = df_tma4_box();
+    return c;
+  }
   if (g.r != 1 || g.var || g.op == 7 || depth > 2) return c;
   const int cols = df_tma_cols(variant), rows = df_tma_rows(variant);
   if (df_tma_smem(g.to, depth, cols, rows) > (size_t)227 * 1024) return c;
@@ -134,9 +144,13 @@ FusedConfig make_fused_config(const Geom &g, int precision, int depth, int varia
 
 FusedConfig choose_fused_config(const Geom &g, int precision, int depth, int bx, int by) {
   int d = depth;
-  // untuned: the depth that measured fastest at 512^3 per precision (double-float:
-  // depth 2, the TMA-staged 64 x 32 region first below)
-  if (d <= 0) d = g.r == 4 ? 2 : ((precision == GIRIH_FP64 || precision == GIRIH_FP64_DF) ? 2 : 4);
+  // untuned: the depth that measured fastest per precision (double-float: depth
+  // 2, the TMA-staged 64 x 32 region first below; at radius 4 one step per pass,
+  // the TMA-staged 32 x 32 tile of operator 0)
+  if (d <= 0) {
+    if (g.r == 4) d = precision == GIRIH_FP64_DF ? 1 : 2;
+    else d = (precision == GIRIH_FP64 || precision == GIRIH_FP64_DF) ? 2 : 4;
+  }
   d = d > fused_max_depth(g, precision) ? fused_max_depth(g, precision) : d;
   // double-float: the TMA-staged variants first (the 64 x 32 region, fastest at
   // 512^3, as the untuned choice), so that a tile they share with a register

@@ -991,9 +991,10 @@ cudaError_t launch_fused_op_impl(const Geom &g, const FusedConfig &cfg, const Fu
       case 4:  // x pairs: 32 x 64 region, 1024 threads (radius 1)
         if constexpr (OpTraits<OP>::R == 1) return launch_variant<OP, T, COMP, 16, 64, 1, 2, TM>(g, L, s);
         break;
-      case 5:  // TMA-staged 32 x 32 and 32 x 64 regions (fused_df_tma.cu)
+      case 5:  // TMA-staged 32 x 32 and 32 x 64 regions (fused_df_tma.cu; operator 0: fused_df_tma4.cu)
       case 6:
         if constexpr (OP == 1 || OP == 8) return launch_fused_df_tma<OP>(g, cfg, L, s);
+        if constexpr (OP == 0) return launch_fused_df_tma4(g, cfg, L, s);
         break;
     }
   } else if constexpr (OpTraits<OP>::R == 1) {  // x pairs: vector loads, stores and shared-memory traffic

@@ -132,7 +132,8 @@ def test_auto_schedule_untuned_defaults():
     operators; double-float), plain elsewhere (FP64 arithmetic, radius 4,
     variable coefficients)."""
     for op, prec, want in ((1, "fp64", gpu.PLAIN), (8, "fp64", gpu.PLAIN), (0, "fp64", gpu.PLAIN),
-                           (8, "fp64df", gpu.FUSED), (1, "mixed", gpu.FUSED), (8, "mixed", gpu.FUSED),
+                           (8, "fp64df", gpu.FUSED), (0, "fp64df", gpu.FUSED), (1, "mixed", gpu.FUSED),
+                           (8, "mixed", gpu.FUSED),
                            (8, "fp32", gpu.FUSED), (0, "mixed", gpu.PLAIN),
                            (5, "fp64", gpu.PLAIN), (5, "mixed", gpu.PLAIN), (4, "mixed", gpu.PLAIN)):
         with gpu.Context(op, 32, 32, 32, precision=prec, schedule="auto") as ctx:
@@ -222,6 +223,38 @@ def test_fused_double_float_tma_equals_register_kernel(op, variant):
             np.testing.assert_array_equal(u2, r2)
             assert max_rel(u1, ref.U1, ref) <= FP64_TOL
             assert max_rel(u2, ref.U2, ref) <= FP64_TOL
+
+
+@pytest.mark.parametrize("shape", [(61, 37, 29), (5, 3, 4), (70, 2, 9), (97, 130, 45), (400, 400, 12)])
+def test_fused_double_float_tma_radius4_equals_register_kernel(shape):
+    """The 25-point leapfrog (operator 0, radius 4) in double-float, one step
+    per pass: the TMA-staged kernel (variant 5 of operator 0, a 32 x 32 tile
+    with 40 x 40 boxes, fused_df_tma4.cu) performs the register kernel's
+    arithmetic in the same order, so results are bit-identical to variant 0
+    (64 x 32 region, 56 x 24 tile).  Covered: odd nt, grids smaller than one
+    box, boxes over every domain edge, and (400 x 400: 169 tiles for 152
+    persistent CTAs) CTAs that take a second piece.  Held to the FP64 bound
+    against the oracle."""
+    op = 0
+    g0 = oracle_grid(op, *shape, seed=41)
+    nt = 7 if shape[0] < 400 else 3
+    ref = g0.copy().run(nt, nthreads=4)
+    with gpu_context(g0.copy(), precision="fp64df", schedule="fused", fusion_depth=1, block=(32, 32)) as ctx, \
+            gpu_context(g0.copy(), precision="fp64df", schedule="fused", fusion_depth=1, block=(56, 24)) as reg:
+        assert ctx.info()["kernel_name"] == "fused_df_tma"
+        assert reg.info()["kernel_name"] == "fused_pass"
+        ctx.run(nt)
+        reg.run(nt)
+        u1, u2 = ctx.download()
+        r1, r2 = reg.download()
+    np.testing.assert_array_equal(u1, r1)
+    np.testing.assert_array_equal(u2, r2)
+    assert max_rel(u1, ref.U1, ref) <= FP64_TOL
+    assert max_rel(u2, ref.U2, ref) <= FP64_TOL
+    # untuned, the double-float form of operator 0 takes this kernel, one step per pass
+    with gpu.Context(op, *shape, precision="fp64df", schedule="fused") as ctx:
+        info = ctx.info()
+        assert (info["kernel_name"], info["fusion_depth"], info["block_x"]) == ("fused_df_tma", 1, 32)
 
 
 def test_fused_double_float_reference_init():

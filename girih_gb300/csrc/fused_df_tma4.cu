@@ -109,26 +109,35 @@ __device__ __forceinline__ unsigned df_tma4_piece(const FusedArgs<Df64> &a, cons
     tma_load_3d(ring_roc2, &maps.roc2, xg, yg, sb - R, &bars[0]);
   }
 
-  for (int s = sb, t = 0; s <= se; s++, t++) {
+  // ring bookkeeping carried from step to step (uniform values; recomputing
+  // them with divisions by the 10-slot ring cost ~30 instructions per update):
+  // kb = slot of plane s, ph = the parity its barrier completes with, kpo =
+  // offset of the old-state / roc2 slot of plane s - R, zs[d] = offset of the
+  // slot of plane s - 2R + d (valid once 2R + 1 planes have arrived)
+  int kb = 0, kpo = 0;
+  unsigned ph = 0;
+  int zs[2 * R + 1];
+#pragma unroll
+  for (int d = 0; d <= 2 * R; d++) zs[d] = 0;
+  for (int s = sb; s <= se; s++) {
+#pragma unroll
+    for (int d = 0; d < 2 * R; d++) zs[d] = zs[d + 1];
+    zs[2 * R] = kb * PLANE;
+    const int kb1 = kb + 1 == NB ? 0 : kb + 1;
     // next plane in flight (its slots were last read at step s - 1, before that
     // step's barrier), then wait for this one
     if (tid == 0 && s + 1 <= se) {
-      const int kb1 = (t + 1) % NB, kp1 = (t + 1) % NP;
       fence_proxy_async_smem();  // earlier generic reads of the slots before the async writes
       mbar_arrive_expect_tx(&bars[kb1], kBytes);
       tma_load_3d(ring_cur + kb1 * PLANE, &maps.cur, xg, yg, s + 1, &bars[kb1]);
-      tma_load_3d(ring_prev + kp1 * PLANE, &maps.prev, xg, yg, s + 1 - R, &bars[kb1]);
-      tma_load_3d(ring_roc2 + kp1 * PLANE, &maps.roc2, xg, yg, s + 1 - R, &bars[kb1]);
+      tma_load_3d(ring_prev + (PLANE - kpo), &maps.prev, xg, yg, s + 1 - R, &bars[kb1]);
+      tma_load_3d(ring_roc2 + (PLANE - kpo), &maps.roc2, xg, yg, s + 1 - R, &bars[kb1]);
     }
-    if (!mbar_wait(&bars[t % NB], (unsigned)(t / NB) & 1u, 1u << 26)) timeout = 1;
+    if (!mbar_wait(&bars[kb], ph, 1u << 26)) timeout = 1;
 
     const int p = s - R;
-    if (p >= Z0) {  // t >= 2R here: planes p - R .. p + R are in slots (t - 2R .. t) mod NB
+    if (p >= Z0) {  // 2R + 1 planes have arrived: planes p - R .. p + R are in zs[0 .. 2R]
       const Df64 *const base = ring_cur + toff;
-      const int kp = (t % NP) * PLANE;
-      int zs[2 * R + 1];
-#pragma unroll
-      for (int d = 0; d <= 2 * R; d++) zs[d] = ((t - 2 * R + d) % NB) * PLANE;
 #pragma unroll
       for (int c = 0; c < 2; c++) {
         if (!(act >> c & 1u)) continue;
@@ -143,8 +152,8 @@ __device__ __forceinline__ unsigned df_tma4_piece(const FusedArgs<Df64> &a, cons
           const Df64 zp = lds(base + zs[R + d] + c * BW) + lds(base + zs[R - d] + c * BW);
           lap = lap + cc[d] * ((xp + yp) + zp);
         }
-        const Df64 uold = lds(ring_prev + kp + toff + c * BW);
-        const Df64 r2 = lds(ring_roc2 + kp + toff + c * BW);
+        const Df64 uold = lds(ring_prev + kpo + toff + c * BW);
+        const Df64 r2 = lds(ring_roc2 + kpo + toff + c * BW);
         const Df64 val = df_norm(twice_minus(centre, uold) + r2 * lap);
         const int64_t o = (int64_t)p * plane + col[c];
         if (in_array(o, 1, g.elems, flag)) {
@@ -158,6 +167,9 @@ __device__ __forceinline__ unsigned df_tma4_piece(const FusedArgs<Df64> &a, cons
       }
     }
     __syncthreads();
+    kb = kb1;
+    ph ^= kb == 0 ? 1u : 0u;
+    kpo = PLANE - kpo;
   }
   return timeout;
 }

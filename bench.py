@@ -614,9 +614,12 @@ def run_secondary(args, local):
         op_info = gpu.OP_INFO[wl["op"]]
         o = {"operator": wl["op"], "grid": [wl["n"]] * 3, "nt": wl["nt"], "seed": wl["seed"], "forms": {}}
         for k, v in res.items():
-            algo = v["bytes_per_lup"] * v["glups"] if v["schedule"] == "plain" else None
+            # one step per pass (plain, or fused at depth 1): the one-step bytes per update are the
+            # pass's algorithmic bytes; deeper passes move fewer and report none here
+            algo = v["bytes_per_lup"] * v["glups"] if (v["schedule"] == "plain" or v["depth"] == 1) else None
             o["forms"][k] = {"glups": v["glups"], "ms_per_step": v["ms_per_step"], "schedule": v["schedule"],
-                             "depth": v["depth"], "tile": v["tile"], "bytes_per_lup": v["bytes_per_lup"],
+                             "kernel": v["kernel"], "depth": v["depth"], "tile": v["tile"],
+                             "bytes_per_lup": v["bytes_per_lup"],
                              "hbm_gbs_algorithmic": algo,
                              "hbm_frac_of_peak": (algo / peak) if algo else None,
                              "errors": errs.get(k)}

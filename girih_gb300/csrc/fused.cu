@@ -72,6 +72,20 @@ static FusedConfig make_box_config(int precision, int depth, int variant) {
   return c;
 }
 
+// Operator 0 (radius 4), variant 5: the TMA-staged one-step pass of
+// fused_df_tma4.cu (32 x 32 tile, 40 x 40 boxes) for `esize`-byte elements; its
+// boxes start at the interior x offset, which must sit on 16 bytes.
+static FusedConfig make_tma4_config(const Geom &g, int esize, int depth, int variant) {
+  FusedConfig c{};
+  if (g.op != 0 || depth != 1 || variant != 5 || (g.ox * esize) % 16) return c;
+  if (tma4_smem(esize) > (size_t)227 * 1024) return c;
+  c.depth = 1;
+  c.variant = 5;
+  c.bx = c.by = tma4_tile();
+  c.box_w = c.box_h = tma4_box();
+  return c;
+}
+
 // Double-float radius-1 constant-coefficient operators (1, 8), variants 5 and 6:
 // the TMA-staged kernel of fused_df_tma.cu (32 rows, 32 or 64 columns, depth
 // <= 2).  Its boxes start on 16 bytes (2 columns), so the tile is the aligned
@@ -79,15 +93,7 @@ static FusedConfig make_box_config(int precision, int depth, int variant) {
 // 0 (radius 4): variant 5 is fused_df_tma4.cu, depth 1, a 32 x 32 tile.
 static FusedConfig make_df_tma_config(const Geom &g, int depth, int variant) {
   FusedConfig c{};
-  if (g.op == 0) {  // radius 4: one step per pass (fused_df_tma4.cu), boxes from an even x
-    if (depth != 1 || variant != 5 || (g.ox & 1)) return c;
-    if (df_tma4_smem() > (size_t)227 * 1024) return c;
-    c.depth = 1;
-    c.variant = 5;
-    c.bx = c.by = df_tma4_tile();
-    c.box_w = c.box_h = df_tma4_box();
-    return c;
-  }
+  if (g.op == 0) return make_tma4_config(g, 8, depth, variant);
   if (g.r != 1 || g.var || g.op == 7 || depth > 2) return c;
   const int cols = df_tma_cols(variant), rows = df_tma_rows(variant);
   if (df_tma_smem(g.to, depth, cols, rows) > (size_t)227 * 1024) return c;
@@ -106,7 +112,7 @@ FusedConfig make_fused_config(const Geom &g, int precision, int depth, int varia
       variant < 0 || variant >= FV_COUNT)
     return c;
   if (g.op == 7) return make_box_config(precision, depth, variant);
-  if (variant >= 5) return precision == GIRIH_FP64_DF ? make_df_tma_config(g, depth, variant) : c;
+  if (variant >= 5) return precision == GIRIH_FP64_DF ? make_df_tma_config(g, depth, variant) : make_tma4_config(g, 4, depth, variant);
   int ntx, ry, vx;
   variant_shape(variant, g.r, precision, &ntx, &ry, &vx);
   if (variant == 2 && precision != GIRIH_FP64_DF && ((g.r == 1 && depth == 4) || (g.r == 4 && depth == 1)))
@@ -203,6 +209,7 @@ cudaError_t launch_fused(const Geom &g, int tsz, int precision, const FusedConfi
 const char *fused_kernel_name(int op, int precision, const FusedConfig &cfg) {
   if (op == 7) return "fused_box_pass";
   if (precision == GIRIH_FP64_DF && cfg.variant >= 5) return "fused_df_tma";
+  if (cfg.variant >= 5) return "fused_f32_tma4";
   return cfg.box_w > 0 ? "fused_pass_tma" : "fused_pass";
 }
 

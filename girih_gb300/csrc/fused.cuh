@@ -44,16 +44,17 @@ __host__ __device__ constexpr size_t df_tma_smem(int to, int tt, int cols, int r
          (size_t)(df_tma_nb(to) + (to == 2 ? 2 + df_tma_nr(tt) : 0)) * cols * rows * 8 + (size_t)df_tma_nb(to) * 8;
 }
 
-// Double-float TMA pass of operator 0 (radius 4, one step per pass;
-// fused_df_tma4.cu), variant 5: output tile 32 x 32 (one column and two
-// adjacent rows per thread), TMA boxes of the tile plus the radius-4 halo
-// (40 x 40); the input state ring holds the 2R + 1 planes an update reads and
-// the one in flight, the old state and roc2 rings 2 slots each.
-__host__ __device__ constexpr int df_tma4_tile() { return 32; }
-__host__ __device__ constexpr int df_tma4_box() { return 40; }
-__host__ __device__ constexpr int df_tma4_nb() { return 10; }
-__host__ __device__ constexpr size_t df_tma4_smem() {
-  return (size_t)(df_tma4_nb() + 4) * df_tma4_box() * df_tma4_box() * 8 + (size_t)df_tma4_nb() * 8;
+// TMA-staged one-step passes of operator 0 (radius 4; fused_df_tma4.cu),
+// variant 5 of the double-float, FP32 and mixed forms: output tile 32 x 32
+// (one column and two adjacent rows per thread), TMA boxes of the tile plus
+// the radius-4 halo (40 x 40); the input state ring holds the 2R + 1 planes an
+// update reads and the one in flight, the old state and roc2 rings 2 slots
+// each.  `esize`: bytes per element (8 double-float, 4 FP32).
+__host__ __device__ constexpr int tma4_tile() { return 32; }
+__host__ __device__ constexpr int tma4_box() { return 40; }
+__host__ __device__ constexpr int tma4_nb() { return 10; }
+__host__ __device__ constexpr size_t tma4_smem(int esize) {
+  return (size_t)(tma4_nb() + 4) * tma4_box() * tma4_box() * esize + (size_t)tma4_nb() * 8;
 }
 
 struct FusedConfig {
@@ -93,8 +94,11 @@ const char *fused_kernel_name(int op, int precision, const FusedConfig &cfg);
 // double-float TMA passes of operators 1 and 8 (fused_df_tma.cu)
 template <int OP>
 cudaError_t launch_fused_df_tma(const Geom &g, const FusedConfig &cfg, const FusedLaunch &L, cudaStream_t s);
-// double-float TMA pass of operator 0 (fused_df_tma4.cu)
+// TMA-staged one-step passes of operator 0 (fused_df_tma4.cu): double-float,
+// and FP32 storage with FP32 (COMP = false) or compensated (mixed) arithmetic
 cudaError_t launch_fused_df_tma4(const Geom &g, const FusedConfig &cfg, const FusedLaunch &L, cudaStream_t s);
+template <bool COMP>
+cudaError_t launch_fused_f32_tma4(const Geom &g, const FusedConfig &cfg, const FusedLaunch &L, cudaStream_t s);
 
 // per-(op, type) launchers defined in the fused_*.cu instantiation files
 template <int OP, class T, bool COMP>

@@ -1025,6 +1025,9 @@ cudaError_t launch_fused_op_impl(const Geom &g, const FusedConfig &cfg, const Fu
         }
         break;
       case 3: if constexpr (kTma) return launch_variant<OP, T, COMP, 32, 32, 2, 1, TM, true>(g, L, s); break;
+      case 5:  // one-step TMA pass of operator 0, 32 x 32 tile (fused_df_tma4.cu)
+        if constexpr (OP == 0 && std::is_same<T, float>::value) return launch_fused_f32_tma4<COMP>(g, cfg, L, s);
+        break;
     }
   }
   return cudaErrorInvalidValue;

@@ -257,6 +257,32 @@ def test_fused_double_float_tma_radius4_equals_register_kernel(shape):
         assert (info["kernel_name"], info["fusion_depth"], info["block_x"]) == ("fused_df_tma", 1, 32)
 
 
+@pytest.mark.parametrize("precision", ["fp32", "mixed"])
+@pytest.mark.parametrize("shape", [(61, 37, 29), (5, 3, 4), (70, 2, 9), (400, 400, 12)])
+def test_fused_fp32_tma_radius4_equals_register_kernel(precision, shape):
+    """The 25-point leapfrog in FP32 storage, one step per pass: the TMA-staged
+    kernel (variant 5 of operator 0, fused_df_tma4.cu; FP32 arithmetic, or the
+    compensated leapfrog of the mixed form) performs the register kernel's
+    arithmetic in the same order: bit-identical to variant 0 (56 x 24 tile),
+    including grids smaller than one box, boxes over every domain edge and
+    CTAs that take a second piece (400 x 400)."""
+    op = 0
+    g0 = oracle_grid(op, *shape, seed=43)
+    nt = 7 if shape[0] < 400 else 3
+    ref = g0.copy().run(nt, nthreads=4)
+    with gpu_context(g0.copy(), precision=precision, schedule="fused", fusion_depth=1, block=(32, 32)) as ctx, \
+            gpu_context(g0.copy(), precision=precision, schedule="fused", fusion_depth=1, block=(56, 24)) as reg:
+        assert ctx.info()["kernel_name"] == "fused_f32_tma4"
+        assert reg.info()["kernel_name"] == "fused_pass"
+        ctx.run(nt)
+        reg.run(nt)
+        u1, u2 = ctx.download()
+        r1, r2 = reg.download()
+    np.testing.assert_array_equal(u1, r1)
+    np.testing.assert_array_equal(u2, r2)
+    assert max_rel(u1, ref.U1, ref) < 5e-6
+
+
 def test_fused_double_float_reference_init():
     """The reference ramp + 100.1 boundary sources (operator 1, default coefficients)."""
     g0 = oracle_grid(1, 45, 31, 27)

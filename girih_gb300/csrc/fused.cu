@@ -73,16 +73,18 @@ static FusedConfig make_box_config(int precision, int depth, int variant) {
 }
 
 // Operator 0 (radius 4), variant 5: the TMA-staged one-step pass of
-// fused_df_tma4.cu (32 x 32 tile, 40 x 40 boxes) for `esize`-byte elements; its
-// boxes start at the interior x offset, which must sit on 16 bytes.
+// fused_df_tma4.cu (32 x 32 tile; 40 x 40 boxes of the input state, 32 x 32 of
+// the old state and roc2) for `esize`-byte elements; the boxes start at x
+// offsets g.ox and g.ox + r, which must sit on 16 bytes.
 static FusedConfig make_tma4_config(const Geom &g, int esize, int depth, int variant) {
   FusedConfig c{};
-  if (g.op != 0 || depth != 1 || variant != 5 || (g.ox * esize) % 16) return c;
+  if (g.op != 0 || depth != 1 || variant != 5 || (g.ox * esize) % 16 || ((g.ox + g.r) * esize) % 16) return c;
   if (tma4_smem(esize) > (size_t)227 * 1024) return c;
   c.depth = 1;
   c.variant = 5;
   c.bx = c.by = tma4_tile();
   c.box_w = c.box_h = tma4_box();
+  c.box2_w = c.box2_h = tma4_tile();
   return c;
 }
 

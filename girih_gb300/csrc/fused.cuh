@@ -47,14 +47,16 @@ __host__ __device__ constexpr size_t df_tma_smem(int to, int tt, int cols, int r
 // TMA-staged one-step passes of operator 0 (radius 4; fused_df_tma4.cu),
 // variant 5 of the double-float, FP32 and mixed forms: output tile 32 x 32
 // (one column and two adjacent rows per thread), TMA boxes of the tile plus
-// the radius-4 halo (40 x 40); the input state ring holds the 2R + 1 planes an
-// update reads and the one in flight, the old state and roc2 rings 2 slots
-// each.  `esize`: bytes per element (8 double-float, 4 FP32).
+// the radius-4 halo (40 x 40) for the input state, of the tile alone for the
+// old state and roc2 (read at the point only); the input state ring holds the
+// 2R + 1 planes an update reads and the one in flight, the old state and roc2
+// rings 2 slots each.  `esize`: bytes per element (8 double-float, 4 FP32).
 __host__ __device__ constexpr int tma4_tile() { return 32; }
 __host__ __device__ constexpr int tma4_box() { return 40; }
 __host__ __device__ constexpr int tma4_nb() { return 10; }
 __host__ __device__ constexpr size_t tma4_smem(int esize) {
-  return (size_t)(tma4_nb() + 4) * tma4_box() * tma4_box() * esize + (size_t)tma4_nb() * 8;
+  return ((size_t)tma4_nb() * tma4_box() * tma4_box() + (size_t)4 * tma4_tile() * tma4_tile()) * esize +
+         (size_t)tma4_nb() * 8;
 }
 
 struct FusedConfig {
@@ -62,6 +64,7 @@ struct FusedConfig {
   int variant = 0;  // FusedVariant
   int bx = 0, by = 0;  // output tile of one CTA
   int box_w = 0, box_h = 0;  // TMA box (region) of the variant, 0 without TMA
+  int box2_w = 0, box2_h = 0;  // box of the old state and roc2 where it differs (0: box_w x box_h)
 };
 
 struct FusedLaunch {
@@ -75,6 +78,7 @@ struct FusedLaunch {
                            // (bit 0, a value outside the FP32 range, is set by the double-float split)
   const void *tma_cur, *tma_prev, *tma_roc2;  // host CUtensorMap objects (TMA variants)
   int tma_box_w, tma_box_h;                   // the box the maps were encoded with
+  int tma_box2_w, tma_box2_h;                 // the old state's and roc2's box
   const void *coef;        // variable coefficients (device layout arrays)
   const float *cscale;     // per-array scales of BF16 coefficients (mixed form)
   const double *src;       // source values per step (null: no source point)

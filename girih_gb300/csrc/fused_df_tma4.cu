@@ -13,8 +13,9 @@
 //     halo (40 x 40 per plane);
 //   * keeps the 2R + 1 planes an update reads, and the one in flight, in a
 //     10-slot ring of the input state, so that every neighbour, z included, is
-//     one shared-memory load; the old state and roc2 of the updated plane come
-//     with the same copy (2-slot rings);
+//     one shared-memory load; the old state and roc2 of the updated plane,
+//     read at the point only, come with the same copy as tile-sized boxes
+//     (2-slot rings);
 //   * carries the ring bookkeeping (slot, barrier parity, the window of z
 //     slots) from step to step: recomputing it with divisions by the 10-slot
 //     ring cost ~20 instructions per update;
@@ -35,18 +36,20 @@ template <class T, int NTX, int NTY> struct Tma4Shape {
   static constexpr int R = 4;
   static constexpr int BX = NTX, BY = 2 * NTY;                // output tile
   static constexpr int BW = BX + 2 * R, BH = BY + 2 * R;      // TMA box
-  static constexpr int PLANE = BW * BH;                       // elements of one ring slot
+  static constexpr int PLANE = BW * BH;                       // elements of one input-ring slot
+  static constexpr int PLANE2 = BX * BY;                      // of one old-state / roc2 slot
   static constexpr int NB = tma4_nb(), NP = 2;                // input ring; old-state and roc2 rings
   static constexpr size_t ES = sizeof(T);                     // Df64: an FP32 pair
   static constexpr size_t off_prev = (size_t)NB * PLANE * ES;
-  static constexpr size_t off_roc2 = off_prev + (size_t)NP * PLANE * ES;
-  static constexpr size_t off_bar = off_roc2 + (size_t)NP * PLANE * ES;
+  static constexpr size_t off_roc2 = off_prev + (size_t)NP * PLANE2 * ES;
+  static constexpr size_t off_bar = off_roc2 + (size_t)NP * PLANE2 * ES;
   static constexpr size_t smem_bytes = off_bar + NB * sizeof(uint64_t);
   static_assert(NB == 2 * R + 2, "the ring holds planes p - R .. p + R and the one in flight");
   static_assert(BX == tma4_tile() && BY == tma4_tile() && BW == tma4_box() && BH == tma4_box(),
                 "host and device tiles differ");
   static_assert(smem_bytes == tma4_smem((int)ES), "host and device shared-memory layouts differ");
-  static_assert(off_prev % 128 == 0 && (PLANE * ES) % 128 == 0, "TMA destinations on 128 bytes");
+  static_assert(off_prev % 128 == 0 && (PLANE * ES) % 128 == 0 && (PLANE2 * ES) % 128 == 0,
+                "TMA destinations on 128 bytes");
 };
 
 // One ring element (checked build: inside the CTA's shared memory).
@@ -84,7 +87,7 @@ template <class T, bool COMP, int NTX, int NTY>
 __device__ __forceinline__ unsigned tma4_piece(const FusedArgs<T> &a, const TmaMaps &maps, int bxi, int byi,
                                                int Z0, int Z1, bool first, unsigned char *smraw) {
   using S = Tma4Shape<T, NTX, NTY>;
-  constexpr int R = S::R, NB = S::NB, BW = S::BW, PLANE = S::PLANE;
+  constexpr int R = S::R, NB = S::NB, BW = S::BW, PLANE = S::PLANE, PLANE2 = S::PLANE2;
   constexpr int64_t SMB = (int64_t)S::smem_bytes;
   unsigned *const flag = a.range_flag;
   const Geom &g = a.g;
@@ -111,13 +114,15 @@ __device__ __forceinline__ unsigned tma4_piece(const FusedArgs<T> &a, const TmaM
   T *const ring_prev = reinterpret_cast<T *>(smraw + S::off_prev);
   T *const ring_roc2 = reinterpret_cast<T *>(smraw + S::off_roc2);
   uint64_t *const bars = reinterpret_cast<uint64_t *>(smraw + S::off_bar);
-  const int toff = (2 * ty + R) * BW + tx + R;  // this thread's row-0 point inside a box
+  const int toff = (2 * ty + R) * BW + tx + R;  // this thread's row-0 point inside an input box
+  const int toff2 = 2 * ty * S::BX + tx;         // and inside an old-state / roc2 box
   auto lds = [&](const T *p) -> T { return tma4_ld(p, smraw, SMB, flag); };
 
-  // box origin: interior point (X0 - R, Y0 - R) in array coordinates; its x
-  // sits on 16 bytes (the host admits this shape only when g.ox does)
-  const int xg = X0 + g.ox, yg = Y0;
-  constexpr unsigned kBytes = (unsigned)(PLANE * S::ES) * 3u;
+  // box origins: interior points (X0 - R, Y0 - R) of the input box and (X0, Y0)
+  // of the others in array coordinates; their x sit on 16 bytes (the host
+  // admits this shape only when g.ox and g.ox + R do)
+  const int xg = X0 + g.ox, yg = Y0, xg2 = xg + R, yg2 = Y0 + R;
+  constexpr unsigned kBytes = (unsigned)((PLANE + 2 * PLANE2) * S::ES);
   unsigned timeout = 0;
   if (tid == 0) {  // every phase restarts at 0; a barrier of an earlier piece is invalidated first
     for (int k = 0; k < NB; k++) {
@@ -130,14 +135,14 @@ __device__ __forceinline__ unsigned tma4_piece(const FusedArgs<T> &a, const TmaM
   if (tid == 0) {  // plane sb, with the old state and roc2 of plane sb - R
     mbar_arrive_expect_tx(&bars[0], kBytes);
     tma_load_3d(ring_cur, &maps.cur, xg, yg, sb, &bars[0]);
-    tma_load_3d(ring_prev, &maps.prev, xg, yg, sb - R, &bars[0]);
-    tma_load_3d(ring_roc2, &maps.roc2, xg, yg, sb - R, &bars[0]);
+    tma_load_3d(ring_prev, &maps.prev, xg2, yg2, sb - R, &bars[0]);
+    tma_load_3d(ring_roc2, &maps.roc2, xg2, yg2, sb - R, &bars[0]);
   }
 
   // ring bookkeeping carried from step to step (uniform values): kb = slot of
-  // plane s, ph = the parity its barrier completes with, kpo = offset of the
-  // old-state / roc2 slot of plane s - R, zs[d] = offset of the slot of plane
-  // s - 2R + d (valid once 2R + 1 planes have arrived)
+  // plane s, ph = the parity its barrier completes with, kpo = offset (0 or
+  // PLANE2) of the old-state / roc2 slot of plane s - R, zs[d] = offset of the
+  // slot of plane s - 2R + d (valid once 2R + 1 planes have arrived)
   int kb = 0, kpo = 0;
   unsigned ph = 0;
   int zs[2 * R + 1];
@@ -154,8 +159,8 @@ __device__ __forceinline__ unsigned tma4_piece(const FusedArgs<T> &a, const TmaM
       fence_proxy_async_smem();  // earlier generic reads of the slots before the async writes
       mbar_arrive_expect_tx(&bars[kb1], kBytes);
       tma_load_3d(ring_cur + kb1 * PLANE, &maps.cur, xg, yg, s + 1, &bars[kb1]);
-      tma_load_3d(ring_prev + (PLANE - kpo), &maps.prev, xg, yg, s + 1 - R, &bars[kb1]);
-      tma_load_3d(ring_roc2 + (PLANE - kpo), &maps.roc2, xg, yg, s + 1 - R, &bars[kb1]);
+      tma_load_3d(ring_prev + (PLANE2 - kpo), &maps.prev, xg2, yg2, s + 1 - R, &bars[kb1]);
+      tma_load_3d(ring_roc2 + (PLANE2 - kpo), &maps.roc2, xg2, yg2, s + 1 - R, &bars[kb1]);
     }
     if (!mbar_wait(&bars[kb], ph, 1u << 26)) timeout = 1;
 
@@ -167,8 +172,8 @@ __device__ __forceinline__ unsigned tma4_piece(const FusedArgs<T> &a, const TmaM
         if (!(act >> c & 1u)) continue;
         const T *const cp = base + zs[R] + c * BW;
         const T centre = lds(cp);
-        const T uold = lds(ring_prev + kpo + toff + c * BW);
-        const T r2 = lds(ring_roc2 + kpo + toff + c * BW);
+        const T uold = lds(ring_prev + kpo + toff2 + c * S::BX);
+        const T r2 = lds(ring_roc2 + kpo + toff2 + c * S::BX);
         T val;
         if constexpr (std::is_same<T, Df64>::value) {
           // star_grouped_sum<4>: c0 v + sum_d c_d ((x pair + y pair) + z pair)
@@ -212,7 +217,7 @@ __device__ __forceinline__ unsigned tma4_piece(const FusedArgs<T> &a, const TmaM
     __syncthreads();
     kb = kb1;
     ph ^= kb == 0 ? 1u : 0u;
-    kpo = PLANE - kpo;
+    kpo = PLANE2 - kpo;
   }
   return timeout;
 }
@@ -249,8 +254,10 @@ static cudaError_t launch_tma4(const void *kern, std::atomic<unsigned long long>
   using S = Tma4Shape<T, NTX, NTY>;
   if (L.src != nullptr || L.steps != 1 || cfg.depth != 1 || cfg.variant != 5 || g.op != 0) return cudaErrorInvalidValue;
   if (!L.tma_cur || !L.tma_prev || !L.tma_roc2) return cudaErrorInvalidValue;
-  // the copies must fill exactly the ring slots this shape sizes, from a 16-byte x
-  if (L.tma_box_w != S::BW || L.tma_box_h != S::BH || (g.ox * (int)S::ES) % 16) return cudaErrorInvalidValue;
+  // the copies must fill exactly the ring slots this shape sizes, from 16-byte x offsets
+  if (L.tma_box_w != S::BW || L.tma_box_h != S::BH || L.tma_box2_w != S::BX || L.tma_box2_h != S::BY ||
+      (g.ox * (int)S::ES) % 16 || ((g.ox + S::R) * (int)S::ES) % 16)
+    return cudaErrorInvalidValue;
   int occ = 1, nsm = 152;
   cudaError_t e = fused_kernel_setup(kern, S::smem_bytes, NTX * NTY, attr_set, &occ, &nsm);
   if (e != cudaSuccess) return e;

@@ -277,14 +277,12 @@ EncodeTiledFn encode_tiled() {
   return fn;
 }
 
-const CUtensorMap *tensor_map(girih_gpu_ctx *c, int arr, const void *base) {
-  // one cache slot per TMA variant of the context's precision: 2 and 3 (FP32
-  // storage) or the double-float 5 and 6
-  const int v = c->fcfg.variant >= 5 ? c->fcfg.variant - 5 : c->fcfg.variant - 2;
+// Tensor map of array `arr` (buffers 0-3, roc2 4) in cache slot v with box bw x bh.
+static const CUtensorMap *tensor_map_box(girih_gpu_ctx *c, int arr, const void *base, int v, int bw, int bh) {
   if (v < 0 || v > 1) return nullptr;
   // re-encode when the box or the array changed: a TMA copy of another width
   // would overrun (or under-fill) the ring slots the kernel sized for its own region
-  if (!c->tmap_ok[arr][v] || c->tmap_box[arr][v][0] != c->fcfg.box_w || c->tmap_box[arr][v][1] != c->fcfg.box_h ||
+  if (!c->tmap_ok[arr][v] || c->tmap_box[arr][v][0] != bw || c->tmap_box[arr][v][1] != bh ||
       c->tmap_base[arr][v] != base) {
     c->tmap_ok[arr][v] = false;
     EncodeTiledFn fn = encode_tiled();
@@ -292,18 +290,28 @@ const CUtensorMap *tensor_map(girih_gpu_ctx *c, int arr, const void *base) {
     const Geom &g = c->g;
     const cuuint64_t dims[3] = {(cuuint64_t)g.px, (cuuint64_t)g.nny, (cuuint64_t)g.nnz};
     const cuuint64_t strides[2] = {(cuuint64_t)g.px * c->tsz, (cuuint64_t)g.px * g.nny * c->tsz};
-    const cuuint32_t box[3] = {(cuuint32_t)c->fcfg.box_w, (cuuint32_t)c->fcfg.box_h, 1};
+    const cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)bh, 1};
     const cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = fn(&c->tmaps[arr][v], c->tsz == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
                     3, const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                     CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return nullptr;
     c->tmap_ok[arr][v] = true;
-    c->tmap_box[arr][v][0] = c->fcfg.box_w;
-    c->tmap_box[arr][v][1] = c->fcfg.box_h;
+    c->tmap_box[arr][v][0] = bw;
+    c->tmap_box[arr][v][1] = bh;
     c->tmap_base[arr][v] = base;
   }
   return &c->tmaps[arr][v];
+}
+
+// The variant's map of `arr`: one cache slot per TMA variant of the context's
+// precision, 2 and 3 (FP32 storage) or 5 and 6.  `second`: the old state's and
+// roc2's box where the variant gives them their own (operator 0's variant 5,
+// which has no variant 6, keeps those maps in the second slot).
+const CUtensorMap *tensor_map(girih_gpu_ctx *c, int arr, const void *base, bool second) {
+  const int v = c->fcfg.variant >= 5 ? c->fcfg.variant - 5 : c->fcfg.variant - 2;
+  if (second && c->fcfg.box2_w > 0) return tensor_map_box(c, arr, base, 1 - v, c->fcfg.box2_w, c->fcfg.box2_h);
+  return tensor_map_box(c, arr, base, v, c->fcfg.box_w, c->fcfg.box_h);
 }
 
 // Extra field buffers for the fused schedule: inputs and outputs of a fused
@@ -431,11 +439,13 @@ int issue_steps_impl(girih_gpu_ctx *c, int steps, int *launches, int *iu1, int *
       L.src_n = c->src_n;
     }
     if (c->fcfg.box_w > 0) {  // TMA variant
-      L.tma_prev = tensor_map(c, *iu1, buf[*iu1]);
-      L.tma_cur = tensor_map(c, *iu2, buf[*iu2]);
-      L.tma_roc2 = c->g.to == 2 ? tensor_map(c, 4, dfp ? c->dfr2 : c->roc2) : L.tma_cur;
+      L.tma_prev = tensor_map(c, *iu1, buf[*iu1], true);
+      L.tma_cur = tensor_map(c, *iu2, buf[*iu2], false);
+      L.tma_roc2 = c->g.to == 2 ? tensor_map(c, 4, dfp ? c->dfr2 : c->roc2, true) : L.tma_cur;
       L.tma_box_w = c->fcfg.box_w;
       L.tma_box_h = c->fcfg.box_h;
+      L.tma_box2_w = c->fcfg.box2_w > 0 ? c->fcfg.box2_w : c->fcfg.box_w;
+      L.tma_box2_h = c->fcfg.box2_h > 0 ? c->fcfg.box2_h : c->fcfg.box_h;
       if (!L.tma_prev || !L.tma_cur || !L.tma_roc2)
         return fail(GIRIH_GPU_ECUDA, "TMA tensor map encoding failed");
     }

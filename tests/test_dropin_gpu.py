@@ -67,8 +67,9 @@ def _report(stdout):
 
 
 @pytest.mark.parametrize("kernel,precision,schedule", [(1, "fp64", "plain"), (1, "fp64df", "fused"),
-                                                       (0, "mixed", "fused"), (5, "mixed", "plain"),
-                                                       (7, "fp64", "plain"), (7, "fp64df", "fused")])
+                                                       (0, "mixed", "fused"), (0, "fp64df", "fused"),
+                                                       (5, "mixed", "plain"), (7, "fp64", "plain"),
+                                                       (7, "fp64df", "fused")])
 def test_performance_run_reports_parse_py_keys(driver, tmp_path, kernel, precision, schedule):
     """The reference's performance harness timing the GPU stepper in each form
     (operator 8 has no reference id, so the reference CLI cannot name it)."""
@@ -83,3 +84,5 @@ def test_performance_run_reports_parse_py_keys(driver, tmp_path, kernel, precisi
     assert js is not None and js["calls"] == 3 and js["target_kernel"] == kernel
     assert js["precision"] == precision and js["schedule"] == schedule
     assert js["glups_device_max"] > 0
+    if (kernel, precision) == (0, "fp64df"):  # the TMA-staged one-step pass of the 25-point operator
+        assert js["kernel"] == "fused_df_tma" and js["fusion_depth"] == 1

@@ -9,8 +9,8 @@
 // the region's threads include the halo, and each of the 25 neighbours goes
 // through the general addressing.  This kernel:
 //   * covers the output tile only (32 x 32: one column and two adjacent rows
-//     per thread, 512 threads); the TMA boxes are the tile plus the radius-4
-//     halo (40 x 40 per plane);
+//     per thread, 512 threads); the input state's TMA boxes are the tile plus
+//     the radius-4 halo (40 x 40 per plane);
 //   * keeps the 2R + 1 planes an update reads, and the one in flight, in a
 //     10-slot ring of the input state, so that every neighbour, z included, is
 //     one shared-memory load; the old state and roc2 of the updated plane,
@@ -24,8 +24,9 @@
 //     df_norm; FP32: apply_op<0>; mixed: leapfrog_compensated of
 //     star_const_sum<4>), so results are bit-identical;
 //   * runs persistent CTAs over the (tile, plane range) pieces of
-//     for_each_piece, each piece paying the ring fill (2R planes) once (FP32:
-//     two CTAs per SM, 90 KB of shared memory each).
+//     for_each_piece, each piece paying the ring fill (2R planes) once
+//     (double-float: one CTA per SM, 161 KB of shared memory; FP32: two, 80 KB
+//     each).
 // At step s of a piece the copy of plane s + 1 is issued and plane s - R is
 // updated; a CTA barrier per step protects the slots the next copy overwrites.
 #include "fused_impl.cuh"
@@ -234,14 +235,14 @@ __device__ __forceinline__ void tma4_pass(const FusedArgs<T> &a, const TmaMaps &
   if (timeout && a.range_flag) atomicOr(a.range_flag, 2u);  // a copy never completed within the wait bound
 }
 
-// Double-float: one CTA per SM (179 KB of shared memory).
+// Double-float: one CTA per SM (161 KB of shared memory).
 template <int NTX, int NTY>
 __global__ void __launch_bounds__(NTX *NTY, 1) fused_df_tma4(FusedArgs<Df64> a, const __grid_constant__ TmaMaps maps) {
   extern __shared__ __align__(128) unsigned char smraw[];
   tma4_pass<Df64, false, NTX, NTY>(a, maps, smraw);
 }
 
-// FP32 storage: two CTAs per SM (90 KB each).
+// FP32 storage: two CTAs per SM (80 KB each).
 template <bool COMP, int NTX, int NTY>
 __global__ void __launch_bounds__(NTX *NTY, 2) fused_f32_tma4(FusedArgs<float> a, const __grid_constant__ TmaMaps maps) {
   extern __shared__ __align__(128) unsigned char smraw[];
